@@ -1,0 +1,200 @@
+"""GB300-native variable-size batched SGEMM.
+
+Python mirror of the C ABI in ``include/bgemm.h`` (``libbgemm_gb300.so``),
+bound with ctypes exactly as a user of the shared library would bind it.  The
+library is the product; this module only loads it, converts arguments and
+raises on non-success statuses.  There is no Python or CPU fallback: if the
+shared library is missing, :func:`lib` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+__all__ = [
+    "BgemmError", "MODES", "lib", "build", "sgemm_vbatched", "Plan", "framework_gemm",
+    "framework_check_device", "device_info", "LIB_PATH",
+]
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libbgemm_gb300.so")
+
+MODES = {"simt": 0, "tf32": 1, "tf32x3": 2, "bf16x3": 3}
+MODE_NAMES = {v: k for k, v in MODES.items()}
+
+STATUS = {
+    0: "BGEMM_SUCCESS", 1: "BGEMM_ERROR_INVALID_VALUE", 2: "BGEMM_ERROR_NOT_SUPPORTED",
+    3: "BGEMM_ERROR_ALLOC", 4: "BGEMM_ERROR_CUDA", 5: "BGEMM_ERROR_DEVICE_TIMEOUT",
+    6: "BGEMM_ERROR_INTERNAL",
+}
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+class BgemmError(RuntimeError):
+    def __init__(self, status: int, arg: int, matrix: int, message: str):
+        self.status, self.arg, self.matrix, self.message = status, arg, matrix, message
+        super().__init__("%s (arg %d, matrix %d): %s" % (STATUS.get(status, status), arg,
+                                                         matrix, message))
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [
+        ("batch", ctypes.c_int), ("mode", ctypes.c_int), ("num_tiles", ctypes.c_int),
+        ("grid", ctypes.c_int), ("tile_config_hist", ctypes.c_int * 16),
+        ("useful_flops", ctypes.c_double), ("min_bytes", ctypes.c_double),
+        ("device_bytes", ctypes.c_size_t), ("workspace_bytes", ctypes.c_size_t),
+    ]
+
+    def as_dict(self):
+        return {
+            "batch": self.batch, "mode": self.mode, "num_tiles": self.num_tiles,
+            "grid": self.grid, "tile_config_hist": list(self.tile_config_hist),
+            "useful_flops": self.useful_flops, "min_bytes": self.min_bytes,
+            "device_bytes": self.device_bytes, "workspace_bytes": self.workspace_bytes,
+        }
+
+
+class PlanOptions(ctypes.Structure):
+    _fields_ = [("force_tile_config", ctypes.c_int), ("max_ctas", ctypes.c_int),
+                ("disable_rebalance", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
+
+
+def build(**kw) -> str:
+    """Compile libbgemm_gb300.so for sm_103a (see builder.py)."""
+    from . import builder
+    return builder.build(**kw)
+
+
+def lib() -> ctypes.CDLL:
+    """Load libbgemm_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libbgemm_gb300.so is not built (run __graft_entry__.build() or "
+                           "python -m batchgemm_gb300.build)")
+    L = ctypes.CDLL(LIB_PATH)
+    i, f, vp = ctypes.c_int, ctypes.c_float, ctypes.c_void_p
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.bgemm_sgemm_vbatched.argtypes = [ip, ip, ip, f, vp, ip, vp, ip, f, vp, ip, i, i, vp]
+    L.bgemm_plan_create.argtypes = [ctypes.POINTER(vp), ip, ip, ip, ip, ip, ip, i, i, vp]
+    L.bgemm_plan_create_ex.argtypes = [ctypes.POINTER(vp), ip, ip, ip, ip, ip, ip, i, i, vp,
+                                       ctypes.POINTER(PlanOptions)]
+    L.bgemm_plan_execute.argtypes = [vp, f, vp, vp, f, vp, vp]
+    L.bgemm_plan_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
+    L.bgemm_plan_check_device.argtypes = [vp, vp]
+    L.bgemm_plan_destroy.argtypes = [vp]
+    L.bgemm_framework_gemm.argtypes = [vp, vp, vp, vp, vp, vp, vp, i, i, vp]
+    L.bgemm_framework_check_device.argtypes = [vp]
+    L.bgemm_last_error_arg.argtypes = [ip]
+    L.bgemm_last_error_arg.restype = i
+    L.bgemm_last_error_message.restype = ctypes.c_char_p
+    L.bgemm_status_string.argtypes = [i]
+    L.bgemm_status_string.restype = ctypes.c_char_p
+    L.bgemm_device_info.argtypes = [ip, ip, ip]
+    L.bgemm_version.restype = i
+    for name in ("bgemm_sgemm_vbatched", "bgemm_plan_create", "bgemm_plan_create_ex",
+                 "bgemm_plan_execute", "bgemm_plan_info", "bgemm_plan_check_device",
+                 "bgemm_plan_destroy", "bgemm_framework_gemm", "bgemm_framework_check_device",
+                 "bgemm_device_info"):
+        getattr(L, name).restype = i
+    _lib = L
+    return L
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        L = lib()
+        m = ctypes.c_int(-1)
+        arg = L.bgemm_last_error_arg(ctypes.byref(m))
+        msg = (L.bgemm_last_error_message() or b"").decode(errors="replace")
+        raise BgemmError(status, arg, m.value, msg)
+
+
+def _iarr(v: Sequence[int]):
+    n = len(v)
+    return (ctypes.c_int * max(n, 1))(*[int(x) for x in v])
+
+
+def _mode(mode) -> int:
+    return MODES[mode] if isinstance(mode, str) else int(mode)
+
+
+def _stream(stream) -> Optional[int]:
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return stream.cuda_stream or None
+    return int(stream) or None
+
+
+def sgemm_vbatched(M, N, K, alpha, dA, lda, dB, ldb, beta, dC, ldc, mode="simt",
+                   stream=None) -> None:
+    """bgemm_sgemm_vbatched: host size arrays, device addresses of the pointer arrays."""
+    _check(lib().bgemm_sgemm_vbatched(_iarr(M), _iarr(N), _iarr(K), float(alpha), dA,
+                                      _iarr(lda), dB, _iarr(ldb), float(beta), dC, _iarr(ldc),
+                                      len(M), _mode(mode), _stream(stream)))
+
+
+class Plan:
+    """bgemm_plan_create / execute / destroy."""
+
+    def __init__(self, M, N, K, lda, ldb, ldc, mode="simt", stream=None,
+                 force_tile_config: int = -1, max_ctas: int = 0, rebalance: bool = True):
+        self._h = ctypes.c_void_p()
+        self.batch = len(M)
+        opt = PlanOptions()
+        opt.force_tile_config = force_tile_config
+        opt.max_ctas = max_ctas
+        opt.disable_rebalance = 0 if rebalance else 1
+        _check(lib().bgemm_plan_create_ex(ctypes.byref(self._h), _iarr(M), _iarr(N), _iarr(K),
+                                          _iarr(lda), _iarr(ldb), _iarr(ldc), len(M),
+                                          _mode(mode), _stream(stream), ctypes.byref(opt)))
+
+    def execute(self, alpha, dA, dB, beta, dC, stream=None) -> None:
+        _check(lib().bgemm_plan_execute(self._h, float(alpha), dA, dB, float(beta), dC,
+                                        _stream(stream)))
+
+    def info(self) -> dict:
+        inf = PlanInfo()
+        _check(lib().bgemm_plan_info(self._h, ctypes.byref(inf)))
+        return inf.as_dict()
+
+    def check_device(self, stream=None) -> None:
+        _check(lib().bgemm_plan_check_device(self._h, _stream(stream)))
+
+    def close(self) -> None:
+        if self._h:
+            _check(lib().bgemm_plan_destroy(self._h))
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def framework_gemm(dM, dN, dK, dA, dB, dC, batch: int, max_dim: int, stream=None,
+                   dT=None) -> None:
+    """Reference drop-in: device size arrays, C_i += A_i B_i (lda=M, ldb=K, ldc=M)."""
+    _check(lib().bgemm_framework_gemm(dM, dN, dK, dA, dB, dC, dT, int(batch), int(max_dim),
+                                      _stream(stream)))
+
+
+def framework_check_device(stream=None) -> None:
+    _check(lib().bgemm_framework_check_device(_stream(stream)))
+
+
+def device_info() -> dict:
+    a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _check(lib().bgemm_device_info(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+    return {"num_sms": a.value, "simt_ctas_per_sm": b.value, "tc_ctas_per_sm": c.value}

@@ -1,0 +1,51 @@
+// bgemm_internal.h -- structures shared by the host planner and the kernels.
+#pragma once
+#include <stdint.h>
+
+#include <cuda_runtime.h>
+
+namespace bgemm {
+
+// Per-matrix descriptor, uploaded once per plan (32 bytes).
+struct MatDesc {
+  int M, N, K;
+  int lda, ldb, ldc;
+  int cfg;    // tile configuration id of the plan's mode
+  int aux;    // tensor-core modes: index of the matrix's packed operands; else 0
+};
+
+// One work item of the largest-first tile queue (8 bytes).
+struct TileItem {
+  int mat;
+  uint16_t tm, tn;  // tile coordinates along M and N (tensor-core swapped
+                    // orientation: along the MMA's M and N)
+};
+
+// ---------------------------------------------------------------- SIMT ----
+// Tile configurations of the FP32 SIMT kernel: 256 threads arranged 16 x 16,
+// each owning a TM x TN register tile.
+struct SimtCfg {
+  int bm, bn, tm, tn;
+};
+constexpr int kSimtNumCfgs = 8;
+constexpr SimtCfg kSimtCfgs[kSimtNumCfgs] = {
+    {16, 16, 1, 1},  {32, 32, 2, 2},  {64, 32, 4, 2},  {32, 64, 2, 4},
+    {64, 64, 4, 4},  {128, 64, 8, 4}, {64, 128, 4, 8}, {128, 128, 8, 8},
+};
+
+struct SimtParams {
+  const MatDesc* descs;
+  const TileItem* items;
+  int n_items;
+  const int* n_items_dev;  // if set, the item count is read from the device
+  int* counters;  // [0]: next work item, [1]: CTAs finished (self-reset)
+  float alpha, beta;
+  const float* const* A;
+  const float* const* B;
+  float* const* C;
+};
+
+cudaError_t simt_launch(const SimtParams& p, int grid, cudaStream_t stream);
+int simt_ctas_per_sm();
+
+}  // namespace bgemm

@@ -1,0 +1,204 @@
+// framework.cu -- drop-in for the reference framework's kernel entry
+//   gemm<<<grid, 256, 16 KB>>>(M, N, K, A, B, C, T_strategy)
+// (CUDA/framework/kernel.h:11, launched at CUDA/framework/gemm.cu:200): the
+// sizes are device arrays, C_i += A_i * B_i column-major with lda = M_i,
+// ldb = K_i, ldc = M_i.
+//
+// Because the sizes live on the device, the tile queue is built there too:
+//   1. fw_plan_kernel (one CTA) picks each matrix's SIMT tile configuration
+//      with the same cost model as the host planner, buckets matrices by
+//      modelled tile time (quarter-octave bins) and reserves each matrix a
+//      contiguous range of the queue, longest tiles first;
+//   2. fw_expand_kernel writes the work items (one warp per matrix);
+//   3. the persistent SIMT kernel reads the item count from the device.
+// The three launches allocate nothing and can be captured in a CUDA graph;
+// the queue scratch is owned by the library (one buffer per device, grown
+// when a call needs more).
+#include <mutex>
+#include <unordered_map>
+
+#include "bgemm.h"
+#include "bgemm_internal.h"
+#include "plan_internal.h"
+#include "tile_table.h"
+
+namespace bgemm {
+namespace {
+
+constexpr int kBins = 64;
+
+__constant__ SimtCfg c_cfgs[kSimtNumCfgs];
+__constant__ TileCost c_cost[kSimtNumCfgs];
+
+struct FwScratch {
+  int* err;         // bit 0: a size was negative or above max_dim
+  int* n_items;
+  int* counters;    // 2 ints: queue head, CTAs finished
+  MatDesc* descs;   // [cap_batch]
+  int* mat_start;   // [cap_batch] first queue slot of each matrix (-1: none)
+  TileItem* items;  // [cap_items]
+};
+
+__global__ void fw_plan_kernel(const int* __restrict__ dM, const int* __restrict__ dN,
+                               const int* __restrict__ dK, int batch, int max_dim,
+                               FwScratch s) {
+  __shared__ int bin_tiles[kBins];
+  __shared__ int bin_start[kBins];
+  for (int b = threadIdx.x; b < kBins; b += blockDim.x) bin_tiles[b] = 0;
+  __syncthreads();
+  // per-matrix choice; the bin and offset are parked in mat_start for now
+  for (int i = threadIdx.x; i < batch; i += blockDim.x) {
+    const int M = dM[i], N = dN[i], K = dK[i];
+    const bool bad = M < 0 || N < 0 || K < 0 || M > max_dim || N > max_dim;
+    if (bad) atomicOr(s.err, 1);
+    int best = -1, bin = 0;
+    long long bt = 0;
+    float btt = 0.f;
+    if (!bad && M > 0 && N > 0) {
+      double bw = 0.0;
+      for (int c = kSimtNumCfgs - 1; c >= 0; --c) {
+        const long long t = (long long)((M + c_cfgs[c].bm - 1) / c_cfgs[c].bm) *
+                            ((N + c_cfgs[c].bn - 1) / c_cfgs[c].bn);
+        const float tt = c_cost[c].a_ns + c_cost[c].b_ns * (float)K;
+        const double w = (double)t * tt;
+        if (best < 0 || w < bw * 0.999) { best = c; bt = t; bw = w; btt = tt; }
+      }
+      bin = min(kBins - 1, max(0, (int)(4.0f * __log2f(fmaxf(btt, 1.0f)) - 24.0f)));
+    }
+    s.descs[i] = MatDesc{M, N, K, max(M, 1), max(K, 1), max(M, 1), best < 0 ? 0 : best,
+                         best < 0 ? 0 : bin};
+    s.mat_start[i] = best < 0 ? -1 : atomicAdd(&bin_tiles[bin], (int)bt);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int b = kBins - 1; b >= 0; --b) {  // longest tiles first
+      bin_start[b] = run;
+      run += bin_tiles[b];
+    }
+    *s.n_items = run;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < batch; i += blockDim.x) {
+    const int off = s.mat_start[i];
+    if (off >= 0) s.mat_start[i] = bin_start[s.descs[i].aux] + off;
+  }
+}
+
+__global__ void fw_expand_kernel(int batch, FwScratch s) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= batch) return;
+  const int start = s.mat_start[warp];
+  if (start < 0) return;
+  const MatDesc d = s.descs[warp];
+  const int tmx = (d.M + c_cfgs[d.cfg].bm - 1) / c_cfgs[d.cfg].bm;
+  const int tnx = (d.N + c_cfgs[d.cfg].bn - 1) / c_cfgs[d.cfg].bn;
+  const int tiles = tmx * tnx;
+  for (int t = lane; t < tiles; t += 32)
+    s.items[start + t] = TileItem{warp, (uint16_t)(t % tmx), (uint16_t)(t / tmx)};
+}
+
+struct FwContext {
+  void* mem = nullptr;
+  size_t cap_batch = 0;
+  size_t cap_items = 0;
+  FwScratch s{};
+  bool consts = false;
+};
+
+std::mutex g_fw_mu;
+std::unordered_map<int, FwContext> g_fw;
+
+}  // namespace
+}  // namespace bgemm
+
+using namespace bgemm;
+
+extern "C" bgemm_status_t bgemm_framework_gemm(const int* dM, const int* dN, const int* dK,
+                                               float* const* dA, float* const* dB,
+                                               float* const* dC, const int* dT, int batch,
+                                               int max_dim, bgemm_stream_t stream) {
+  (void)dT;  // tile choice is this library's own
+  if (batch < 0) return set_error(BGEMM_ERROR_INVALID_VALUE, 8, -1, "batch < 0");
+  if (batch == 0) return BGEMM_SUCCESS;
+  if (!dM) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "M is NULL");
+  if (!dN) return set_error(BGEMM_ERROR_INVALID_VALUE, 2, -1, "N is NULL");
+  if (!dK) return set_error(BGEMM_ERROR_INVALID_VALUE, 3, -1, "K is NULL");
+  if (!dA) return set_error(BGEMM_ERROR_INVALID_VALUE, 4, -1, "A is NULL");
+  if (!dB) return set_error(BGEMM_ERROR_INVALID_VALUE, 5, -1, "B is NULL");
+  if (!dC) return set_error(BGEMM_ERROR_INVALID_VALUE, 6, -1, "C is NULL");
+  if (max_dim < 1 || max_dim > (1 << 20))
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 9, -1, "max_dim = %d not in [1, 2^20]",
+                     max_dim);
+  DeviceFacts df;
+  bgemm_status_t st = device_facts(&df);
+  if (st != BGEMM_SUCCESS) return st;
+
+  const size_t per = (size_t)((max_dim + 15) / 16);
+  const size_t need_items = (size_t)batch * per * per;
+  std::lock_guard<std::mutex> lk(g_fw_mu);
+  FwContext& ctx = g_fw[df.device];
+  if (!ctx.consts) {
+    cudaError_t e = cudaMemcpyToSymbol(c_cfgs, kSimtCfgs, sizeof(kSimtCfgs));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_cost, kSimtCost, sizeof(kSimtCost));
+    if (e != cudaSuccess) return cuda_error(e, "framework constants");
+    ctx.consts = true;
+  }
+  if ((size_t)batch > ctx.cap_batch || need_items > ctx.cap_items) {
+    const size_t cb = std::max((size_t)batch, ctx.cap_batch);
+    const size_t ci = std::max(need_items, ctx.cap_items);
+    const size_t off_descs = 256;
+    const size_t off_start = off_descs + ((sizeof(MatDesc) * cb + 255) & ~size_t(255));
+    const size_t off_items = off_start + ((sizeof(int) * cb + 255) & ~size_t(255));
+    const size_t total = off_items + sizeof(TileItem) * ci;
+    if (ctx.mem) cudaFree(ctx.mem);  // waits for kernels still using it
+    ctx.mem = nullptr;
+    ctx.cap_batch = ctx.cap_items = 0;
+    cudaError_t e = cudaMalloc(&ctx.mem, total);
+    if (e != cudaSuccess)
+      return set_error(BGEMM_ERROR_ALLOC, 0, -1, "framework queue of %zu bytes: %s", total,
+                       cudaGetErrorString(e));
+    e = cudaMemset(ctx.mem, 0, 256);
+    if (e != cudaSuccess) return cuda_error(e, "framework queue init");
+    char* b = static_cast<char*>(ctx.mem);
+    ctx.s.err = reinterpret_cast<int*>(b);
+    ctx.s.n_items = reinterpret_cast<int*>(b + 4);
+    ctx.s.counters = reinterpret_cast<int*>(b + 128);
+    ctx.s.descs = reinterpret_cast<MatDesc*>(b + off_descs);
+    ctx.s.mat_start = reinterpret_cast<int*>(b + off_start);
+    ctx.s.items = reinterpret_cast<TileItem*>(b + off_items);
+    ctx.cap_batch = cb;
+    ctx.cap_items = ci;
+  }
+  fw_plan_kernel<<<1, 1024, 0, stream>>>(dM, dN, dK, batch, max_dim, ctx.s);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "framework plan kernel");
+  fw_expand_kernel<<<(batch + 7) / 8, 256, 0, stream>>>(batch, ctx.s);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "framework expand kernel");
+  SimtParams sp{ctx.s.descs, ctx.s.items, 0, ctx.s.n_items, ctx.s.counters, 1.0f, 1.0f,
+                const_cast<const float* const*>(dA), const_cast<const float* const*>(dB), dC};
+  e = simt_launch(sp, df.num_sms * df.simt_ctas_per_sm, stream);
+  if (e != cudaSuccess) return cuda_error(e, "framework SIMT launch");
+  return BGEMM_SUCCESS;
+}
+
+extern "C" bgemm_status_t bgemm_framework_check_device(bgemm_stream_t stream) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaError_t e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_error(e, "cudaStreamSynchronize");
+  std::lock_guard<std::mutex> lk(g_fw_mu);
+  auto it = g_fw.find(dev);
+  if (it == g_fw.end() || !it->second.mem) return BGEMM_SUCCESS;
+  int err = 0;
+  e = cudaMemcpy(&err, it->second.s.err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_error(e, "framework error word");
+  if (err) {
+    cudaMemset(it->second.s.err, 0, sizeof(int));
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1,
+                     "a matrix size was negative or above max_dim; such matrices were skipped");
+  }
+  return BGEMM_SUCCESS;
+}

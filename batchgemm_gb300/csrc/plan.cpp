@@ -1,0 +1,592 @@
+// plan.cpp -- host side of the C ABI: argument checks, the per-matrix tiling
+// heuristic, the largest-first tile queue, descriptor upload and launch.
+//
+// Rewrites of the reference's host driver (CUDA/framework/gemm.cu):
+//   - per-matrix tile choice (gemm.cu:107-118: largest tile dividing M and N)
+//     becomes a cost-model choice over tiles that handle ragged edges;
+//   - the "wavefront" demotion loop (gemm.cu:121-169: demote every matrix of
+//     the largest strategy while total parallelism is below a threshold)
+//     becomes a rebalance that splits the longest tiles until none exceeds
+//     the average load of one persistent CTA;
+//   - the dense (max tiles M, max tiles N, batch) grid (gemm.cu:181-196)
+//     becomes a queue of only the real tiles, ordered largest-first, pulled
+//     by one wave of persistent CTAs;
+//   - the six synchronous cudaMemcpy uploads (gemm.cu:57-77, 172-174) become
+//     one asynchronous copy of a packed descriptor block from pinned memory.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <list>
+#include <mutex>
+#include <queue>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "bgemm.h"
+#include "bgemm_debug.h"
+#include "bgemm_internal.h"
+#include "plan_internal.h"
+#include "tile_table.h"
+
+namespace bgemm {
+
+// ------------------------------------------------------------- errors ----
+static thread_local int t_err_arg = 0;
+static thread_local int t_err_mat = -1;
+static thread_local char t_err_msg[512] = "";
+
+bgemm_status_t set_error(bgemm_status_t st, int arg, int mat, const char* fmt, ...) {
+  t_err_arg = arg;
+  t_err_mat = mat;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(t_err_msg, sizeof(t_err_msg), fmt, ap);
+  va_end(ap);
+  return st;
+}
+void clear_error() {
+  t_err_arg = 0;
+  t_err_mat = -1;
+  t_err_msg[0] = 0;
+}
+bgemm_status_t cuda_error(cudaError_t e, const char* what) {
+  return set_error(BGEMM_ERROR_CUDA, 0, -1, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// -------------------------------------------------------- device facts ----
+bgemm_status_t device_facts(DeviceFacts* out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+  static std::mutex mu;
+  static std::unordered_map<int, DeviceFacts> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(dev);
+  if (it != cache.end()) {
+    *out = it->second;
+    return BGEMM_SUCCESS;
+  }
+  DeviceFacts f{};
+  f.device = dev;
+  int major = 0, minor = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  cudaDeviceGetAttribute(&f.num_sms, cudaDevAttrMultiProcessorCount, dev);
+  f.cc = major * 10 + minor;
+  if (f.cc != 103)
+    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 0, -1,
+                     "device %d has compute capability %d.%d; this library is built for "
+                     "sm_103a (GB300) only",
+                     dev, major, minor);
+  f.simt_ctas_per_sm = simt_ctas_per_sm();
+  f.tc_ctas_per_sm = 1;
+  cache[dev] = f;
+  *out = f;
+  return BGEMM_SUCCESS;
+}
+
+// ------------------------------------------------------------ planning ----
+static inline long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
+
+// Candidate (cost, tiles) of configuration c for matrix (M, N, K).
+static inline void simt_eval(int c, int M, int N, int K, long long* tiles, double* t_tile) {
+  const SimtCfg& g = kSimtCfgs[c];
+  *tiles = ceil_div(M, g.bm) * ceil_div(N, g.bn);
+  *t_tile = kSimtCost[c].a_ns + kSimtCost[c].b_ns * (double)K;
+}
+
+static bgemm_status_t choose_simt(const int* M, const int* N, const int* K, int batch, int slots,
+                                  const bgemm_plan_options_t* opt, std::vector<MatPlan>& mp) {
+  mp.assign(batch, MatPlan{-1, 0, 0.0});
+  double total = 0.0;
+  for (int i = 0; i < batch; ++i) {
+    if (M[i] == 0 || N[i] == 0) continue;
+    int best = -1;
+    long long bt = 0;
+    double bw = 0, btt = 0;
+    for (int c = kSimtNumCfgs - 1; c >= 0; --c) {
+      if (opt && opt->force_tile_config >= 0 && c != opt->force_tile_config) continue;
+      long long t;
+      double tt;
+      simt_eval(c, M[i], N[i], K[i], &t, &tt);
+      const double w = (double)t * tt;
+      if (best < 0 || w < bw * 0.999) {
+        best = c; bt = t; bw = w; btt = tt;
+      }
+    }
+    if (bt > 65535LL * 65535LL || ceil_div(M[i], kSimtCfgs[best].bm) > 65535 ||
+        ceil_div(N[i], kSimtCfgs[best].bn) > 65535)
+      return set_error(BGEMM_ERROR_NOT_SUPPORTED, 1, i, "matrix %d: too many tiles", i);
+    mp[i] = MatPlan{best, bt, btt};
+    total += bw;
+  }
+  if (opt && (opt->disable_rebalance || opt->force_tile_config >= 0)) return BGEMM_SUCCESS;
+  // Rebalance: while the longest tile is longer than the average load of a
+  // persistent CTA, move the matrix owning it to the configuration with the
+  // shortest tile among those that do not raise its total time by more than
+  // the parallelism gained.
+  using Entry = std::pair<double, int>;
+  std::priority_queue<Entry> heap;
+  for (int i = 0; i < batch; ++i)
+    if (mp[i].cfg >= 0) heap.push({mp[i].t_tile, i});
+  int guard = 8 * batch + 64;
+  while (!heap.empty() && guard-- > 0) {
+    const auto [tt, i] = heap.top();
+    if (tt != mp[i].t_tile) { heap.pop(); continue; }
+    if (tt <= total / slots) break;
+    // best alternative with a shorter tile
+    int best = -1;
+    long long bt = 0;
+    double btt = 0, bw = 0;
+    for (int c = 0; c < kSimtNumCfgs; ++c) {
+      long long t;
+      double t2;
+      simt_eval(c, M[i], N[i], K[i], &t, &t2);
+      if (t2 >= tt || t <= mp[i].tiles) continue;
+      const double w = (double)t * t2;
+      if (best < 0 || w < bw) { best = c; bt = t; btt = t2; bw = w; }
+    }
+    heap.pop();
+    if (best < 0) continue;
+    const double old_w = (double)mp[i].tiles * mp[i].t_tile;
+    const double new_total = total - old_w + bw;
+    // accept if the makespan bound improves
+    const double before = std::max(total / slots, tt);
+    const double after = std::max(new_total / slots, btt);
+    if (after >= before) continue;
+    total = new_total;
+    mp[i] = MatPlan{best, bt, btt};
+    heap.push({btt, i});
+  }
+  return BGEMM_SUCCESS;
+}
+
+static bgemm_status_t check_args(const int* M, const int* N, const int* K, const int* lda,
+                                 const int* ldb, const int* ldc, int batch, int mode,
+                                 int arg_M, int arg_N, int arg_K, int arg_lda, int arg_ldb,
+                                 int arg_ldc, int arg_batch, int arg_mode) {
+  if (batch < 0) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_batch, -1, "batch < 0");
+  if (mode < BGEMM_MODE_SIMT_FP32 || mode > BGEMM_MODE_BF16X3)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, arg_mode, -1, "unknown mode %d", mode);
+  if (batch == 0) return BGEMM_SUCCESS;
+  if (!M) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_M, -1, "M is NULL");
+  if (!N) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_N, -1, "N is NULL");
+  if (!K) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_K, -1, "K is NULL");
+  if (!lda) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_lda, -1, "lda is NULL");
+  if (!ldb) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_ldb, -1, "ldb is NULL");
+  if (!ldc) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_ldc, -1, "ldc is NULL");
+  for (int i = 0; i < batch; ++i) {
+    if (M[i] < 0) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_M, i, "M[%d] = %d < 0", i, M[i]);
+    if (N[i] < 0) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_N, i, "N[%d] = %d < 0", i, N[i]);
+    if (K[i] < 0) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_K, i, "K[%d] = %d < 0", i, K[i]);
+    if (lda[i] < std::max(1, M[i]))
+      return set_error(BGEMM_ERROR_INVALID_VALUE, arg_lda, i, "lda[%d] = %d < max(1, M = %d)", i,
+                       lda[i], M[i]);
+    if (ldb[i] < std::max(1, K[i]))
+      return set_error(BGEMM_ERROR_INVALID_VALUE, arg_ldb, i, "ldb[%d] = %d < max(1, K = %d)", i,
+                       ldb[i], K[i]);
+    if (ldc[i] < std::max(1, M[i]))
+      return set_error(BGEMM_ERROR_INVALID_VALUE, arg_ldc, i, "ldc[%d] = %d < max(1, M = %d)", i,
+                       ldc[i], M[i]);
+  }
+  return BGEMM_SUCCESS;
+}
+
+// Queue order: matrices by modelled tile time, longest first (the
+// longest-processing-time rule over one wave of persistent CTAs).  Returns
+// the number of work items.
+static long long order_matrices(const std::vector<MatPlan>& mp, std::vector<int>& order) {
+  order.clear();
+  long long n_items = 0;
+  for (int i = 0; i < (int)mp.size(); ++i)
+    if (mp[i].cfg >= 0) {
+      order.push_back(i);
+      n_items += mp[i].tiles;
+    }
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return mp[a].t_tile > mp[b].t_tile; });
+  return n_items;
+}
+
+// Writes the work items; each matrix's tiles stay together (n outer, m
+// inner) so consecutive items share operand panels in L2.
+static void expand_items(int mode, bgemm_plan_s* p, const int* M, const int* N,
+                         const std::vector<MatPlan>& mp, const std::vector<int>& order,
+                         MatDesc* hd, TileItem* hi) {
+  size_t w = 0;
+  for (int i : order) {
+    int bm, bn;
+    if (mode == BGEMM_MODE_SIMT_FP32) {
+      bm = kSimtCfgs[mp[i].cfg].bm;
+      bn = kSimtCfgs[mp[i].cfg].bn;
+    } else {
+      tc_tile_dims(p, i, M[i], N[i], mp[i].cfg, &bm, &bn, &hd[i]);
+    }
+    const bool swap = (hd[i].aux & kTcSwapFlag) != 0;
+    const int tmx = (int)ceil_div(swap ? N[i] : M[i], bm);
+    const int tnx = (int)ceil_div(swap ? M[i] : N[i], bn);
+    for (int tn = 0; tn < tnx; ++tn)
+      for (int tm = 0; tm < tmx; ++tm) hi[w++] = TileItem{i, (uint16_t)tm, (uint16_t)tn};
+  }
+}
+
+// Host-only replay of the SIMT planner (tests and the autotuner use it; no
+// GPU needed).  Returns the number of items, or -1 on error / overflow.
+int debug_simt_queue(const int* M, const int* N, const int* K, int batch, int slots,
+                     int force_cfg, int rebalance, int* cfg_out, int* items_out,
+                     int max_items) {
+  bgemm_plan_options_t opt{};
+  opt.force_tile_config = force_cfg;
+  opt.disable_rebalance = rebalance ? 0 : 1;
+  std::vector<MatPlan> mp;
+  if (choose_simt(M, N, K, batch, std::max(slots, 1), &opt, mp) != BGEMM_SUCCESS) return -1;
+  std::vector<int> order;
+  const long long n = order_matrices(mp, order);
+  if (cfg_out)
+    for (int i = 0; i < batch; ++i) cfg_out[i] = mp[i].cfg;
+  if (!items_out) return (int)n;
+  if (n > max_items) return -1;
+  std::vector<MatDesc> hd(batch);
+  for (int i = 0; i < batch; ++i) hd[i] = MatDesc{M[i], N[i], K[i], 0, 0, 0, mp[i].cfg, 0};
+  std::vector<TileItem> it((size_t)n);
+  expand_items(BGEMM_MODE_SIMT_FP32, nullptr, M, N, mp, order, hd.data(), it.data());
+  for (long long t = 0; t < n; ++t) {
+    items_out[3 * t] = it[t].mat;
+    items_out[3 * t + 1] = it[t].tm;
+    items_out[3 * t + 2] = it[t].tn;
+  }
+  return (int)n;
+}
+
+static void free_plan_memory(bgemm_plan_s* p) {
+  if (p->d_mem) cudaFree(p->d_mem);
+  if (p->h_pinned) cudaFreeHost(p->h_pinned);
+  if (p->tc) tc_plan_release(p);
+  p->d_mem = nullptr;
+  p->h_pinned = nullptr;
+}
+
+bgemm_status_t plan_create(bgemm_plan_t* out, const int* M, const int* N, const int* K,
+                           const int* lda, const int* ldb, const int* ldc, int batch, int mode,
+                           cudaStream_t stream, const bgemm_plan_options_t* opt) {
+  if (!out) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
+  *out = nullptr;
+  bgemm_status_t st = check_args(M, N, K, lda, ldb, ldc, batch, mode, 2, 3, 4, 5, 6, 7, 8, 9);
+  if (st != BGEMM_SUCCESS) return st;
+  DeviceFacts df;
+  st = device_facts(&df);
+  if (st != BGEMM_SUCCESS) return st;
+
+  auto* p = new bgemm_plan_s();
+  p->batch = batch;
+  p->mode = mode;
+  p->facts = df;
+  p->info.batch = batch;
+  p->info.mode = mode;
+
+  std::vector<MatPlan> mp;
+  if (mode == BGEMM_MODE_SIMT_FP32) {
+    const int slots = df.num_sms * df.simt_ctas_per_sm;
+    st = choose_simt(M, N, K, batch, slots, opt, mp);
+  } else {
+    st = tc_choose(p, M, N, K, batch, opt, mp);
+  }
+  if (st != BGEMM_SUCCESS) {
+    delete p;
+    return st;
+  }
+
+  std::vector<int> order;
+  const long long n_items = order_matrices(mp, order);
+  if (n_items > (1LL << 31) - 1024) {
+    delete p;
+    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 0, -1, "batch has %lld tiles", n_items);
+  }
+  p->n_items = (int)n_items;
+
+  // host staging layout: [counters 256 B][descs][items][mode extras]
+  const size_t off_desc = 256;
+  const size_t off_items = off_desc + ((sizeof(MatDesc) * (size_t)batch + 255) & ~size_t(255));
+  const size_t end_items = off_items + ((sizeof(TileItem) * (size_t)n_items + 255) & ~size_t(255));
+  size_t total = end_items;
+  size_t tc_extra = 0;
+  if (mode != BGEMM_MODE_SIMT_FP32) tc_extra = tc_extra_bytes(p, batch);
+  total += tc_extra;
+
+  cudaError_t e = cudaMallocHost(&p->h_pinned, end_items);
+  if (e != cudaSuccess) {
+    delete p;
+    return set_error(BGEMM_ERROR_ALLOC, 0, -1, "pinned staging of %zu bytes: %s", end_items,
+                     cudaGetErrorString(e));
+  }
+  e = cudaMalloc(&p->d_mem, total);
+  if (e != cudaSuccess) {
+    free_plan_memory(p);
+    delete p;
+    return set_error(BGEMM_ERROR_ALLOC, 0, -1, "device plan memory of %zu bytes: %s", total,
+                     cudaGetErrorString(e));
+  }
+  char* h = static_cast<char*>(p->h_pinned);
+  std::memset(h, 0, 256);
+  auto* hd = reinterpret_cast<MatDesc*>(h + off_desc);
+  auto* hi = reinterpret_cast<TileItem*>(h + off_items);
+  double flops = 0, bytes = 0;
+  for (int i = 0; i < batch; ++i) {
+    hd[i] = MatDesc{M[i], N[i], K[i], lda[i], ldb[i], ldc[i], mp[i].cfg < 0 ? 0 : mp[i].cfg, 0};
+    flops += 2.0 * M[i] * (double)N[i] * K[i];
+    bytes += 4.0 * ((double)M[i] * K[i] + (double)K[i] * N[i] + (double)M[i] * N[i]);
+    if (mp[i].cfg >= 0 && mp[i].cfg < 16) p->info.tile_config_hist[mp[i].cfg]++;
+  }
+  expand_items(mode, p, M, N, mp, order, hd, hi);
+  p->d_counters = reinterpret_cast<int*>(static_cast<char*>(p->d_mem));
+  p->d_descs = reinterpret_cast<MatDesc*>(static_cast<char*>(p->d_mem) + off_desc);
+  p->d_items = reinterpret_cast<TileItem*>(static_cast<char*>(p->d_mem) + off_items);
+  p->d_extra = static_cast<char*>(p->d_mem) + end_items;
+
+  e = cudaMemcpyAsync(p->d_mem, p->h_pinned, end_items, cudaMemcpyHostToDevice, stream);
+  if (e != cudaSuccess) {
+    free_plan_memory(p);
+    delete p;
+    return cuda_error(e, "descriptor upload");
+  }
+  const int ctas_per_sm = (mode == BGEMM_MODE_SIMT_FP32) ? df.simt_ctas_per_sm : df.tc_ctas_per_sm;
+  long long grid = (long long)df.num_sms * ctas_per_sm;
+  if (opt && opt->max_ctas > 0) grid = std::min<long long>(grid, opt->max_ctas);
+  grid = std::min<long long>(grid, std::max<long long>(n_items, 1));
+  p->grid = (int)grid;
+
+  p->info.num_tiles = p->n_items;
+  p->info.grid = p->grid;
+  p->info.useful_flops = flops;
+  p->info.min_bytes = bytes;
+  p->info.device_bytes = total;
+  if (mode != BGEMM_MODE_SIMT_FP32) {
+    st = tc_plan_finish(p, stream);
+    if (st != BGEMM_SUCCESS) {
+      free_plan_memory(p);
+      delete p;
+      return st;
+    }
+  }
+  *out = p;
+  return BGEMM_SUCCESS;
+}
+
+bgemm_status_t plan_execute(bgemm_plan_t p, float alpha, const float* const* dA,
+                            const float* const* dB, float beta, float* const* dC,
+                            cudaStream_t stream) {
+  if (!p) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
+  if (p->n_items == 0) return BGEMM_SUCCESS;
+  if (!dA) return set_error(BGEMM_ERROR_INVALID_VALUE, 3, -1, "dA is NULL");
+  if (!dB) return set_error(BGEMM_ERROR_INVALID_VALUE, 4, -1, "dB is NULL");
+  if (!dC) return set_error(BGEMM_ERROR_INVALID_VALUE, 6, -1, "dC is NULL");
+  if (p->mode == BGEMM_MODE_SIMT_FP32) {
+    SimtParams sp{p->d_descs, p->d_items, p->n_items, nullptr, p->d_counters, alpha, beta, dA, dB, dC};
+    cudaError_t e = simt_launch(sp, p->grid, stream);
+    if (e != cudaSuccess) return cuda_error(e, "SIMT launch");
+    return BGEMM_SUCCESS;
+  }
+  return tc_execute(p, alpha, dA, dB, beta, dC, stream);
+}
+
+bgemm_status_t plan_destroy(bgemm_plan_t p) {
+  if (!p) return BGEMM_SUCCESS;
+  free_plan_memory(p);
+  delete p;
+  return BGEMM_SUCCESS;
+}
+
+// ---------------------------------------------------------- plan cache ----
+namespace {
+struct PlanCache {
+  std::mutex mu;
+  std::list<std::string> lru;  // front = most recent
+  std::unordered_map<std::string, std::pair<bgemm_plan_t, std::list<std::string>::iterator>> map;
+  static constexpr size_t kMax = 32;
+  ~PlanCache() {
+    // plans are intentionally leaked at process exit: the CUDA context may
+    // already be gone, and freeing into it would fail.
+  }
+};
+PlanCache& cache() {
+  static PlanCache* c = new PlanCache();
+  return *c;
+}
+}  // namespace
+
+bgemm_status_t cached_plan(bgemm_plan_t* out, const int* M, const int* N, const int* K,
+                           const int* lda, const int* ldb, const int* ldc, int batch, int mode,
+                           cudaStream_t stream) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::string key;
+  key.resize(sizeof(int) * (3 + 6 * (size_t)batch) + sizeof(void*));
+  char* k = &key[0];
+  int hdr[3] = {dev, mode, batch};
+  std::memcpy(k, hdr, sizeof(hdr));
+  k += sizeof(hdr);
+  void* sp = stream;
+  std::memcpy(k, &sp, sizeof(void*));
+  k += sizeof(void*);
+  for (const int* a : {M, N, K, lda, ldb, ldc}) {
+    std::memcpy(k, a, sizeof(int) * (size_t)batch);
+    k += sizeof(int) * (size_t)batch;
+  }
+  PlanCache& c = cache();
+  std::lock_guard<std::mutex> lk(c.mu);
+  auto it = c.map.find(key);
+  if (it != c.map.end()) {
+    c.lru.splice(c.lru.begin(), c.lru, it->second.second);
+    *out = it->second.first;
+    return BGEMM_SUCCESS;
+  }
+  bgemm_plan_t p = nullptr;
+  bgemm_status_t st = plan_create(&p, M, N, K, lda, ldb, ldc, batch, mode, stream, nullptr);
+  if (st != BGEMM_SUCCESS) return st;
+  if (c.map.size() >= PlanCache::kMax) {
+    const std::string& victim = c.lru.back();
+    auto vit = c.map.find(victim);
+    if (vit != c.map.end()) {
+      plan_destroy(vit->second.first);  // cudaFree waits for in-flight work
+      c.map.erase(vit);
+    }
+    c.lru.pop_back();
+  }
+  c.lru.push_front(key);
+  c.map.emplace(key, std::make_pair(p, c.lru.begin()));
+  *out = p;
+  return BGEMM_SUCCESS;
+}
+
+}  // namespace bgemm
+
+// ================================================================ C ABI ====
+using namespace bgemm;
+
+extern "C" {
+
+bgemm_status_t bgemm_sgemm_vbatched(const int* M, const int* N, const int* K, float alpha,
+                                    const float* const* dA, const int* lda,
+                                    const float* const* dB, const int* ldb, float beta,
+                                    float* const* dC, const int* ldc, int batch,
+                                    bgemm_mode_t mode, bgemm_stream_t stream) {
+  clear_error();
+  bgemm_status_t st =
+      check_args(M, N, K, lda, ldb, ldc, batch, (int)mode, 1, 2, 3, 6, 8, 11, 12, 13);
+  if (st != BGEMM_SUCCESS || batch == 0) return st;
+  bool any = false;
+  for (int i = 0; i < batch && !any; ++i) any = M[i] > 0 && N[i] > 0;
+  if (!any) return BGEMM_SUCCESS;
+  if (!dA) return set_error(BGEMM_ERROR_INVALID_VALUE, 5, -1, "dA is NULL");
+  if (!dB) return set_error(BGEMM_ERROR_INVALID_VALUE, 7, -1, "dB is NULL");
+  if (!dC) return set_error(BGEMM_ERROR_INVALID_VALUE, 10, -1, "dC is NULL");
+  bgemm_plan_t p = nullptr;
+  st = cached_plan(&p, M, N, K, lda, ldb, ldc, batch, (int)mode, stream);
+  if (st != BGEMM_SUCCESS) return st;
+  st = plan_execute(p, alpha, dA, dB, beta, dC, stream);
+  if (st != BGEMM_SUCCESS && t_err_arg == 0) return st;
+  // plan_execute numbers its own arguments; map them to this entry point
+  if (st == BGEMM_ERROR_INVALID_VALUE) {
+    const int map[7] = {0, 0, 0, 5, 7, 0, 10};
+    if (t_err_arg >= 0 && t_err_arg < 7 && map[t_err_arg]) t_err_arg = map[t_err_arg];
+  }
+  return st;
+}
+
+bgemm_status_t bgemm_plan_create(bgemm_plan_t* plan, const int* M, const int* N, const int* K,
+                                 const int* lda, const int* ldb, const int* ldc, int batch,
+                                 bgemm_mode_t mode, bgemm_stream_t stream) {
+  clear_error();
+  return plan_create(plan, M, N, K, lda, ldb, ldc, batch, (int)mode, stream, nullptr);
+}
+
+bgemm_status_t bgemm_plan_create_ex(bgemm_plan_t* plan, const int* M, const int* N,
+                                    const int* K, const int* lda, const int* ldb,
+                                    const int* ldc, int batch, bgemm_mode_t mode,
+                                    bgemm_stream_t stream, const bgemm_plan_options_t* options) {
+  clear_error();
+  if (options && options->force_tile_config >= 0) {
+    const int ncfg = (mode == BGEMM_MODE_SIMT_FP32) ? kSimtNumCfgs : kTcNumCfgs;
+    if (options->force_tile_config >= ncfg)
+      return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1, "force_tile_config %d >= %d",
+                       options->force_tile_config, ncfg);
+  }
+  return plan_create(plan, M, N, K, lda, ldb, ldc, batch, (int)mode, stream, options);
+}
+
+bgemm_status_t bgemm_plan_execute(bgemm_plan_t plan, float alpha, const float* const* dA,
+                                  const float* const* dB, float beta, float* const* dC,
+                                  bgemm_stream_t stream) {
+  clear_error();
+  return plan_execute(plan, alpha, dA, dB, beta, dC, stream);
+}
+
+bgemm_status_t bgemm_plan_info(bgemm_plan_t plan, bgemm_plan_info_t* info) {
+  clear_error();
+  if (!plan) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
+  if (!info) return set_error(BGEMM_ERROR_INVALID_VALUE, 2, -1, "info is NULL");
+  *info = plan->info;
+  return BGEMM_SUCCESS;
+}
+
+bgemm_status_t bgemm_plan_check_device(bgemm_plan_t plan, bgemm_stream_t stream) {
+  clear_error();
+  if (!plan) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
+  cudaError_t e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_error(e, "cudaStreamSynchronize");
+  if (plan->mode == BGEMM_MODE_SIMT_FP32) return BGEMM_SUCCESS;
+  return tc_check_device(plan, stream);
+}
+
+bgemm_status_t bgemm_plan_destroy(bgemm_plan_t plan) {
+  clear_error();
+  return plan_destroy(plan);
+}
+
+int bgemm_last_error_arg(int* matrix) {
+  if (matrix) *matrix = t_err_mat;
+  return t_err_arg;
+}
+
+const char* bgemm_last_error_message(void) { return t_err_msg; }
+
+const char* bgemm_status_string(bgemm_status_t s) {
+  switch (s) {
+    case BGEMM_SUCCESS: return "BGEMM_SUCCESS";
+    case BGEMM_ERROR_INVALID_VALUE: return "BGEMM_ERROR_INVALID_VALUE";
+    case BGEMM_ERROR_NOT_SUPPORTED: return "BGEMM_ERROR_NOT_SUPPORTED";
+    case BGEMM_ERROR_ALLOC: return "BGEMM_ERROR_ALLOC";
+    case BGEMM_ERROR_CUDA: return "BGEMM_ERROR_CUDA";
+    case BGEMM_ERROR_DEVICE_TIMEOUT: return "BGEMM_ERROR_DEVICE_TIMEOUT";
+    case BGEMM_ERROR_INTERNAL: return "BGEMM_ERROR_INTERNAL";
+  }
+  return "BGEMM_STATUS_UNKNOWN";
+}
+
+bgemm_status_t bgemm_device_info(int* num_sms, int* simt_ctas_per_sm, int* tc_ctas_per_sm) {
+  clear_error();
+  DeviceFacts f;
+  bgemm_status_t st = device_facts(&f);
+  if (st != BGEMM_SUCCESS) return st;
+  if (num_sms) *num_sms = f.num_sms;
+  if (simt_ctas_per_sm) *simt_ctas_per_sm = f.simt_ctas_per_sm;
+  if (tc_ctas_per_sm) *tc_ctas_per_sm = f.tc_ctas_per_sm;
+  return BGEMM_SUCCESS;
+}
+
+int bgemm_version(void) { return 100; }
+
+int bgemm_debug_simt_queue(const int* M, const int* N, const int* K, int batch, int slots,
+                           int force_cfg, int rebalance, int* cfg_out, int* items_out,
+                           int max_items) {
+  clear_error();
+  if (batch < 0 || (batch > 0 && (!M || !N || !K))) return -1;
+  for (int i = 0; i < batch; ++i)
+    if (M[i] < 0 || N[i] < 0 || K[i] < 0) return -1;
+  return debug_simt_queue(M, N, K, batch, slots, force_cfg, rebalance, cfg_out, items_out,
+                          max_items);
+}
+
+}  // extern "C"

@@ -1,0 +1,327 @@
+// simt_kernel.cu -- persistent FP32 SIMT kernel for column-major vbatched SGEMM.
+//
+// Replaces the reference's dense-grid dispatcher (CUDA/framework/kernel.h:11-43,
+// launched over (max tiles M, max tiles N, batch) at CUDA/framework/gemm.cu:181-200)
+// and its tile bodies (CUDA/framework/kernel_128_new.h, kernel_256_new.h,
+// CUDA/batching/kernel_256.h): one wave of persistent CTAs pulls work items
+// from a largest-first tile queue with an atomic counter, so no CTA is
+// launched for a tile outside its matrix.
+//
+// Each item is one BM x BN output tile of one matrix.  256 threads form a
+// 16 x 16 grid; each owns a TM x TN register tile.  Operands stream through a
+// 4-stage cp.async ring of BK = 8 k-slices:
+//   A slice: [k][BM]     (column of A, 16-byte cp.async when lda % 4 == 0 and
+//                         A is 16-byte aligned, 4-byte otherwise)
+//   B slice: [k][BN + 4] (transposed on the way in by 4-byte cp.async; the
+//                         +4 pad keeps the scattered writes conflict-free)
+// Edges are zero-filled by the cp.async source size, so any M, N, K >= 0 and
+// any leading dimension work.  Every output element is a single fma chain
+// over k in order (bit-exact with the reference's tile bodies and with the
+// oracle).  The epilogue stores float4 columns when C allows it; otherwise a
+// warp-shuffle transpose turns each half-warp's 4-element runs into
+// contiguous 64-byte stores.
+#include <stdint.h>
+
+#include "bgemm_internal.h"
+
+namespace bgemm {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kBK = 8;
+constexpr int kStages = 4;
+constexpr int kPadB = 4;
+constexpr int kMaxStageFloats = kBK * (128 + 128 + kPadB);
+constexpr int kSmemBytes = kStages * kMaxStageFloats * 4;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <int W>
+struct VecLd;
+template <>
+struct VecLd<1> {
+  static __device__ __forceinline__ void ld(const float* p, float* v) { v[0] = p[0]; }
+};
+template <>
+struct VecLd<2> {
+  static __device__ __forceinline__ void ld(const float* p, float* v) {
+    const float2 t = *reinterpret_cast<const float2*>(p);
+    v[0] = t.x; v[1] = t.y;
+  }
+};
+template <>
+struct VecLd<4> {
+  static __device__ __forceinline__ void ld(const float* p, float* v) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  }
+};
+
+template <int BM, int BN, int TM, int TN>
+__device__ __forceinline__ void simt_tile(const MatDesc& d, int tm, int tn,
+                                          const float* __restrict__ A,
+                                          const float* __restrict__ B, float* __restrict__ C,
+                                          float alpha, float beta, float* smem) {
+  constexpr int TX = BM / TM;
+  constexpr int TY = BN / TN;
+  static_assert(TX == 16 && TY == 16, "256 threads as 16 x 16");
+  constexpr int TMH = TM > 4 ? 4 : TM;  // contiguous run per half along m
+  constexpr int TNH = TN > 4 ? 4 : TN;
+  constexpr int HM = TM / TMH;          // halves along m (2 for TM = 8)
+  constexpr int HN = TN / TNH;
+  constexpr int LDBS = BN + kPadB;
+  constexpr int A_STAGE = kBK * BM;
+  constexpr int STAGE = A_STAGE + kBK * LDBS;
+
+  const int tid = threadIdx.x;
+  const int tx = tid % TX, ty = tid / TX;
+  const int M = d.M, N = d.N, K = d.K;
+  const long long lda = d.lda, ldb = d.ldb, ldc = d.ldc;
+  const int m0 = tm * BM, n0 = tn * BN;
+  const bool inplace = (alpha == 1.0f && beta == 1.0f);
+
+  // element (i, j) of the register tile sits at
+  //   m = m0 + (i / TMH) * (BM / 2) + tx * TMH + i % TMH
+  //   n = n0 + (j / TNH) * (BN / 2) + ty * TNH + j % TNH
+  auto row_of = [&](int i) { return m0 + (i / TMH) * (BM / HM) + tx * TMH + (i % TMH); };
+  auto col_of = [&](int j) { return n0 + (j / TNH) * (BN / HN) + ty * TNH + (j % TNH); };
+
+  float acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      float v = 0.0f;
+      if (inplace) {
+        const int m = row_of(i), n = col_of(j);
+        if (m < M && n < N) v = C[n * ldc + m];
+      }
+      acc[i][j] = v;
+    }
+
+  const int nkb = (K + kBK - 1) / kBK;
+  const bool a_vec = ((reinterpret_cast<uintptr_t>(A) & 15u) == 0) && ((d.lda & 3) == 0);
+
+  auto load_stage = [&](int kb, int slot) {
+    float* sA = smem + slot * STAGE;
+    float* sB = sA + A_STAGE;
+    const int k0 = kb * kBK;
+    if (a_vec) {
+      constexpr int CH = BM * kBK / 4;
+#pragma unroll
+      for (int c0 = 0; c0 < CH; c0 += kThreads) {
+        const int c = c0 + tid;
+        if (CH % kThreads == 0 || c < CH) {
+          const int mm = (c % (BM / 4)) * 4, kk = c / (BM / 4);
+          const int gm = m0 + mm, gk = k0 + kk;
+          int valid = (gk < K) ? min(max(M - gm, 0), 4) : 0;
+          const float* src = valid ? A + gk * lda + gm : A;
+          cp_async16(smem_u32(sA + kk * BM + mm), src, valid * 4);
+        }
+      }
+    } else {
+      constexpr int EL = BM * kBK;
+#pragma unroll
+      for (int e0 = 0; e0 < EL; e0 += kThreads) {
+        const int e = e0 + tid;
+        if (EL % kThreads == 0 || e < EL) {
+          const int mm = e % BM, kk = e / BM;
+          const int gm = m0 + mm, gk = k0 + kk;
+          const bool v = (gk < K) && (gm < M);
+          cp_async4(smem_u32(sA + kk * BM + mm), v ? A + gk * lda + gm : A, v ? 4 : 0);
+        }
+      }
+    }
+    constexpr int EB = BN * kBK;
+#pragma unroll
+    for (int e0 = 0; e0 < EB; e0 += kThreads) {
+      const int e = e0 + tid;
+      if (EB % kThreads == 0 || e < EB) {
+        const int kk = e % kBK, nn = e / kBK;
+        const int gk = k0 + kk, gn = n0 + nn;
+        const bool v = (gk < K) && (gn < N);
+        cp_async4(smem_u32(sB + kk * LDBS + nn), v ? B + gn * ldb + gk : B, v ? 4 : 0);
+      }
+    }
+  };
+
+#pragma unroll
+  for (int s = 0; s < kStages - 1; ++s) {
+    if (s < nkb) load_stage(s, s);
+    cp_async_commit();
+  }
+
+  for (int kb = 0; kb < nkb; ++kb) {
+    cp_async_wait<kStages - 2>();
+    __syncthreads();
+    {
+      const int nk = kb + kStages - 1;
+      if (nk < nkb) load_stage(nk, nk % kStages);
+      cp_async_commit();
+    }
+    const float* sA = smem + (kb % kStages) * STAGE;
+    const float* sB = sA + A_STAGE;
+#pragma unroll
+    for (int k = 0; k < kBK; ++k) {
+      float a[TM], b[TN];
+#pragma unroll
+      for (int h = 0; h < HM; ++h) VecLd<TMH>::ld(sA + k * BM + h * (BM / HM) + tx * TMH, a + h * TMH);
+#pragma unroll
+      for (int h = 0; h < HN; ++h) VecLd<TNH>::ld(sB + k * LDBS + h * (BN / HN) + ty * TNH, b + h * TNH);
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+  }
+  cp_async_wait<0>();
+
+  // ---- epilogue ----
+  const bool c_vec = (TMH == 4) && ((reinterpret_cast<uintptr_t>(C) & 15u) == 0) &&
+                     ((d.ldc & 3) == 0);
+  const int lane = tid & 31;
+#pragma unroll
+  for (int j = 0; j < TN; ++j) {
+    const int n = col_of(j);
+    const bool n_ok = n < N;
+    float* Ccol = C + n * ldc;
+#pragma unroll
+    for (int h = 0; h < HM; ++h) {
+      const int mb = m0 + h * (BM / HM) + tx * TMH;
+      float v[TMH];
+#pragma unroll
+      for (int r = 0; r < TMH; ++r) v[r] = acc[h * TMH + r][j];
+      if (c_vec) {
+        if (n_ok) {
+          if (mb + TMH <= M) {
+            float4* p = reinterpret_cast<float4*>(Ccol + mb);
+            float4 o;
+            if (inplace) {
+              o = make_float4(v[0], v[1], v[2], v[3]);
+            } else if (beta == 0.0f) {
+              o = make_float4(alpha * v[0], alpha * v[1], alpha * v[2], alpha * v[3]);
+            } else {
+              const float4 c = *p;
+              o = make_float4(fmaf(alpha, v[0], beta * c.x), fmaf(alpha, v[1], beta * c.y),
+                              fmaf(alpha, v[2], beta * c.z), fmaf(alpha, v[3], beta * c.w));
+            }
+            *p = o;
+          } else {
+#pragma unroll
+            for (int r = 0; r < TMH; ++r) {
+              const int m = mb + r;
+              if (m < M) {
+                float* p = Ccol + m;
+                *p = inplace ? v[r] : (beta == 0.0f ? alpha * v[r] : fmaf(alpha, v[r], beta * *p));
+              }
+            }
+          }
+        }
+      } else {
+        // Warp-shuffle transpose: in round q, lane tx of each half-warp writes
+        // m = base + q*16 + tx, taking it from the lane that owns it.
+#pragma unroll
+        for (int q = 0; q < TMH; ++q) {
+          const int ml = q * 16 + tx;
+          const int src = (lane & 16) | (ml / TMH);
+          const int rsel = ml % TMH;
+          float x = 0.0f;
+#pragma unroll
+          for (int r = 0; r < TMH; ++r) {
+            const float t = __shfl_sync(0xffffffffu, v[r], src);
+            if (r == rsel) x = t;
+          }
+          const int m = m0 + h * (BM / HM) + ml;
+          if (n_ok && m < M) {
+            float* p = Ccol + m;
+            *p = inplace ? x : (beta == 0.0f ? alpha * x : fmaf(alpha, x, beta * *p));
+          }
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 2) simt_persistent_kernel(const SimtParams p) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ int s_item;
+  const int n_items = p.n_items_dev ? *p.n_items_dev : p.n_items;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(p.counters, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= n_items) break;
+    const TileItem ti = p.items[it];
+    const MatDesc d = p.descs[ti.mat];
+    const float* A = p.A[ti.mat];
+    const float* B = p.B[ti.mat];
+    float* C = p.C[ti.mat];
+    switch (d.cfg) {
+      case 0: simt_tile<16, 16, 1, 1>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 1: simt_tile<32, 32, 2, 2>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 2: simt_tile<64, 32, 4, 2>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 3: simt_tile<32, 64, 2, 4>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 4: simt_tile<64, 64, 4, 4>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 5: simt_tile<128, 64, 8, 4>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 6: simt_tile<64, 128, 4, 8>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      default: simt_tile<128, 128, 8, 8>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+    }
+    __syncthreads();
+  }
+  // The last CTA to leave resets the queue, so the next launch (or graph
+  // replay) starts from item 0 without a memset.
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(reinterpret_cast<unsigned*>(p.counters) + 1, 1u);
+    if (prev == gridDim.x - 1) {
+      atomicExch(p.counters, 0);
+      atomicExch(p.counters + 1, 0);
+      __threadfence();
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t simt_launch(const SimtParams& p, int grid, cudaStream_t stream) {
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(simt_persistent_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
+  }
+  simt_persistent_kernel<<<grid, kThreads, kSmemBytes, stream>>>(p);
+  return cudaGetLastError();
+}
+
+int simt_ctas_per_sm() {
+  int n = 0;
+  cudaFuncSetAttribute(simt_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       kSmemBytes);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, simt_persistent_kernel, kThreads,
+                                                    kSmemBytes) != cudaSuccess)
+    return 1;
+  return n > 0 ? n : 1;
+}
+
+}  // namespace bgemm

@@ -1,0 +1,442 @@
+"""Benchmark of variable-size batched SGEMM on GB300.
+
+Headline workload: the skewed batch (4000 column-major matrices, 90 % with
+M, N, K uniform in [8, 64] and 10 % uniform in [512, 2048], N(0, 1) entries,
+alpha = 1, beta = 0), run by one persistent kernel per step from a
+CUDA-graph replay.  ``value`` is useful TFLOP/s (sum 2MNK / time) with inputs
+resident in HBM; ``e2e`` is the same metric through the one-shot C-ABI call
+with host buffers (pinned host -> device copies of A and B, device -> host
+copy of C inside the timed region).  The FP32 SIMT form is timed on the same
+batch beside the headline mode.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--mode tf32x3|simt|tf32|bf16x3]
+  python bench.py --impl reference ...   # the CPU loop on the host cores
+
+N > 1 (torchrun, one rank per GPU) runs independent replicas: matrices of a
+batch are independent, so each rank owns a whole batch and no collective
+touches the data path (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "vbatched SGEMM TFLOP/s: 3xTF32 persistent vs FP32-SIMT on GB300 at FP32-level err"
+UNIT = "TFLOP/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default=os.environ.get("BGEMM_BENCH_MODE", "tf32x3"))
+    ap.add_argument("--workload", default="skewed_4000")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the other modes")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ dist --
+def dist_init(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("BGEMM_BENCH_BACKEND") != "gloo"
+                                else "gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world, device):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- clocks --
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        busy = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ CPU oracle --
+def cpu_sample(w, budget_s=15.0, threads=None):
+    """Times the CPU FP32 loop (the oracle port; the reference ships no CPU
+    loop) on a bounded sample of the workload's matrices: all threads, whole
+    matrices, largest-first pool.  Returns (TFLOP/s, cores, description)."""
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    rng = np.random.default_rng(123)
+    order = rng.permutation(w.batch)
+    # grow the sample until it holds ~budget_s of work at a probe rate
+    probe = [i for i in order[:64]]
+    chosen, fl = [], 0.0
+    rate = None
+    for attempt in range(2):
+        if rate is None:
+            target = 2e9  # first probe: ~2 GFLOP
+        else:
+            target = rate * budget_s
+        chosen, fl = [], 0.0
+        for i in order:
+            f = 2.0 * w.M[i] * w.N[i] * w.K[i]
+            if fl + f > target and chosen:
+                continue
+            chosen.append(int(i))
+            fl += f
+            if fl >= target:
+                break
+        Ms = [w.M[i] for i in chosen]
+        Ns = [w.N[i] for i in chosen]
+        Ks = [w.K[i] for i in chosen]
+        As = [rng.standard_normal(max(m * k, 1)).astype(np.float32) for m, k in zip(Ms, Ks)]
+        Bs = [rng.standard_normal(max(k * n, 1)).astype(np.float32) for k, n in zip(Ks, Ns)]
+        Cs = [np.zeros(max(m * n, 1), np.float32) for m, n in zip(Ms, Ns)]
+        t0 = time.perf_counter()
+        used = oracle.vbatched_f32(Ms, Ns, Ks, w.alpha, As, [max(1, m) for m in Ms], Bs,
+                                   [max(1, k) for k in Ks], w.beta, Cs, [max(1, m) for m in Ms],
+                                   nthreads=threads)
+        dt = time.perf_counter() - t0
+        rate = fl / dt
+    desc = ("%d of %d matrices (%.2f GFLOP, random subset, whole matrices), FP32 fma loop, "
+            "%d threads, %.1f s" % (len(chosen), w.batch, fl / 1e9, used, dt))
+    return rate / 1e12, used, desc
+
+
+# ---------------------------------------------------------------- GPU leg --
+def fp64_sampled_error(db, per_matrix=4, seed=0):
+    """Normalised error |c - c64| / sum|a b| on sampled entries, FP64 on the GPU."""
+    import torch
+    rng = np.random.default_rng(seed)
+    idx_m, idx_n, mats = [], [], []
+    for i in range(db.batch):
+        if db.M[i] and db.N[i] and db.K[i]:
+            for _ in range(per_matrix):
+                mats.append(i)
+                idx_m.append(int(rng.integers(0, db.M[i])))
+                idx_n.append(int(rng.integers(0, db.N[i])))
+    if not mats:
+        return 0.0, 0.0, 0
+    kmax = max(db.K[i] for i in mats)
+    S = len(mats)
+    dev = db.A.device
+    errs = []
+    chunk = max(1, (1 << 26) // kmax)
+    for s0 in range(0, S, chunk):
+        ss = range(s0, min(S, s0 + chunk))
+        K = torch.tensor([db.K[mats[s]] for s in ss], device=dev)
+        ar = torch.arange(kmax, device=dev)
+        mask = ar[None, :] < K[:, None]
+        ka = torch.where(mask, ar[None, :], 0)
+        offA = torch.tensor([db.offA[mats[s]] + idx_m[s] for s in ss], device=dev)
+        lda = torch.tensor([db.lda[mats[s]] for s in ss], device=dev)
+        offB = torch.tensor([db.offB[mats[s]] + idx_n[s] * db.ldb[mats[s]] for s in ss],
+                            device=dev)
+        a = db.A[offA[:, None] + ka * lda[:, None]].double()
+        b = db.B[offB[:, None] + ka].double()
+        prod = torch.where(mask, a * b, torch.zeros_like(a))
+        exact = prod.sum(1)
+        absb = prod.abs().sum(1)
+        offC = torch.tensor([db.offC[mats[s]] + idx_m[s] + idx_n[s] * db.ldc[mats[s]]
+                             for s in ss], device=dev)
+        c = db.C[offC].double()
+        errs.append(((c - exact).abs() / absb.clamp_min(1e-300)).cpu())
+    e = torch.cat(errs)
+    return float(e.max()), float(e.mean()), S
+
+
+def gpu_leg(args, rank, world, local):
+    import torch
+    import batchgemm_gb300 as bg
+    from batchgemm_gb300 import workloads
+    from batchgemm_gb300.batch import DeviceBatch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    bg.lib()
+    w = workloads.CONFIGS[args.workload](0)
+    flops = w.flops()
+    db = DeviceBatch(w.M, w.N, w.K, device=str(dev)).fill_fast(w.dist, seed=rank)
+    s = torch.cuda.Stream(device=dev)
+    peaks = {}
+    pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    num_sms = bg.device_info()["num_sms"]
+
+    def time_mode(mode, steps, warmup, sample_clocks=False):
+        with torch.cuda.stream(s):
+            plan = db.plan(mode, stream=s)
+        info = plan.info()
+        # warm-up outside the graph, then capture one step
+        for _ in range(max(1, min(warmup, 2))):
+            db.execute(plan, w.alpha, w.beta, stream=s)
+        s.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            db.execute(plan, w.alpha, w.beta, stream=s)
+        with torch.cuda.stream(s):
+            for _ in range(warmup):
+                g.replay()
+        s.synchronize()
+        barrier(world)
+        torch.cuda.synchronize(dev)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        clk = ClockSampler(local) if sample_clocks else None
+        if clk:
+            clk.__enter__()
+            time.sleep(0.3)
+        with torch.cuda.stream(s):
+            ev0.record(s)
+            for _ in range(steps):
+                g.replay()
+            ev1.record(s)
+        s.synchronize()
+        if clk:
+            clk.__exit__(None, None, None)
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        ms = ev0.elapsed_time(ev1) / steps
+        plan.check_device(stream=s)
+        del g
+        return plan, info, ms, (clk.summary() if clk else None)
+
+    out = {}
+    plan, info, ms, clocks = time_mode(args.mode, args.steps, args.warmup, sample_clocks=True)
+    ms_max = max_over_ranks(ms, world, dev)
+    value = world * flops / (ms_max * 1e-3) / 1e12
+    err_max, err_mean, nsamp = fp64_sampled_error(db)
+    launches_per_step = 1 if args.mode == "simt" else 3
+    out.update(value=value, ms=ms_max, info=info, clocks=clocks, err=(err_max, err_mean, nsamp),
+               launches=launches_per_step * args.steps)
+    plan.close()
+
+    # other modes on the same batch (a few steps each)
+    extra = {}
+    if not args.no_extra:
+        for mode in ("simt", "tf32x3", "tf32", "bf16x3"):
+            if mode == args.mode:
+                continue
+            try:
+                p2, inf2, ms2, _ = time_mode(mode, max(3, args.steps // 4), 3)
+                e2 = fp64_sampled_error(db)
+                extra[mode] = {"tflops": round(flops / (ms2 * 1e-3) / 1e12, 3),
+                               "ms_per_step": round(ms2, 4),
+                               "err_vs_fp64_max": e2[0], "err_vs_fp64_mean": e2[1]}
+                p2.close()
+            except bg.BgemmError as e:
+                extra[mode] = {"unavailable": e.message}
+    out["extra"] = extra
+
+    # roofline of the dominant kernel
+    mode = args.mode
+    clk_max = (clocks or {}).get("sm_max_mhz") or 2070.0
+    if mode == "simt":
+        peak = num_sms * 128 * 2 * clk_max * 1e6 / 1e12
+        out["roofline"] = {"bound": "fp32_simt", "achieved": round(value / world, 3),
+                           "peak": round(peak, 2), "unit": "TFLOP/s",
+                           "frac": round(value / world / peak, 4), "traffic": None,
+                           "peak_source": "SMs x 128 FP32 lanes x 2 x max SM clock (of device "
+                                          "properties; no measured FP32 peak)"}
+    else:
+        bf16 = peaks.get("bf16_tflops", 1900.0)
+        src = "of measured" if "bf16_tflops" in peaks else "of fallback"
+        tf32_peak = bf16 / 2.0
+        mult = 3.0 if mode in ("tf32x3", "bf16x3") else 1.0
+        pipe_peak = bf16 if mode == "bf16x3" else tf32_peak
+        pipe = mult * value / world
+        out["roofline"] = {"bound": "tensor", "achieved": round(pipe, 2),
+                           "peak": round(pipe_peak, 1), "unit": "TFLOP/s",
+                           "frac": round(pipe / pipe_peak, 4), "traffic": None,
+                           "peak_source": "%s bf16 dense %s%s" % (
+                               src, "" if mode == "bf16x3" else "/ 2 (TF32 rate)",
+                               "; achieved counts the 3 tensor products" if mult > 1 else "")}
+
+    # end to end through the one-shot C-ABI call with host buffers
+    if not args.no_e2e:
+        hA = torch.empty(db.A.numel(), dtype=torch.float32, pin_memory=True)
+        hB = torch.empty(db.B.numel(), dtype=torch.float32, pin_memory=True)
+        hC = torch.empty(db.C.numel(), dtype=torch.float32, pin_memory=True)
+        hA.copy_(db.A)
+        hB.copy_(db.B)
+        h2d = (hA.numel() + hB.numel()) * 4
+        if w.beta != 0:
+            h2d += hC.numel() * 4
+        d2h = hC.numel() * 4
+
+        def e2e_step():
+            with torch.cuda.stream(s):
+                db.A.copy_(hA, non_blocking=True)
+                db.B.copy_(hB, non_blocking=True)
+                if w.beta != 0:
+                    db.C.copy_(hC, non_blocking=True)
+                db.run(mode, w.alpha, w.beta, stream=s)
+                hC.copy_(db.C, non_blocking=True)
+
+        for _ in range(2):
+            e2e_step()
+        s.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        esteps = max(3, args.steps // 4)
+        with torch.cuda.stream(s):
+            e0.record(s)
+        for _ in range(esteps):
+            e2e_step()
+        with torch.cuda.stream(s):
+            e1.record(s)
+        s.synchronize()
+        barrier(world)
+        ems = max_over_ranks(e0.elapsed_time(e1) / esteps, world, dev)
+        out["e2e"] = {"value": round(world * flops / (ems * 1e-3) / 1e12, 4), "unit": UNIT,
+                      "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                      "ms_per_step": round(ems, 3), "api": "bgemm_sgemm_vbatched (host copies "
+                                                           "pinned)"}
+    return w, out
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_init(args.gpus)
+    from batchgemm_gb300 import workloads
+    w = workloads.CONFIGS[args.workload](0)
+    config = {"workload": w.name, "desc": w.desc, "batch": w.batch,
+              "useful_gflop_per_step": round(w.flops() / 1e9, 3),
+              "mode": args.mode if args.impl == "ours" else "fp32 CPU loop",
+              "l2": "inputs (%.1f GB) larger than the 129 MB L2; no flush" % (w.bytes() / 1e9),
+              "parallelism": "replicas x%d" % world}
+
+    if args.impl == "reference":
+        # the reference ships no CPU implementation; its stand-in is the CPU
+        # restatement of its fma loop (oracle/), timed on the host cores.
+        if rank != 0:
+            return
+        vals = []
+        desc = ""
+        cores = 0
+        for _ in range(args.warmup):
+            pass
+        steps = max(1, min(args.steps, 3))
+        for _ in range(steps):
+            v, cores, desc = cpu_sample(w, budget_s=8.0)
+            vals.append(v)
+        value = statistics.median(vals)
+        line = {"metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": world,
+                "steps": steps, "warmup": args.warmup, "ms_per_step": round(
+                    w.flops() / (value * 1e12) * 1e3, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "impl": "reference", "config": config,
+                "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": cores,
+                                 "kind": "port", "sample": desc},
+                "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    w, out = gpu_leg(args, rank, world, local)
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        v, cores, desc = cpu_sample(w, budget_s=12.0)
+        cpu = {"value": round(v, 6), "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+    dtype = {"simt": "f32", "tf32": "tf32", "tf32x3": "tf32x3 (f32 in/out)",
+             "bf16x3": "bf16x3 (f32 in/out)"}[args.mode]
+    line = {
+        "metric": METRIC, "value": round(out["value"], 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(out["ms"], 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+        "data": "synthetic (seeded on device)", "config": config,
+        "roofline": out["roofline"], "cpu_baseline": cpu, "clocks": out["clocks"],
+        "gpu_launches": out["launches"],
+        "err_vs_fp64": {"max": out["err"][0], "mean": out["err"][1], "samples": out["err"][2],
+                        "normalised_by": "sum_k |a_mk b_kn|"},
+        "plan": {"tiles": out["info"]["num_tiles"], "grid": out["info"]["grid"],
+                 "cfg_hist": out["info"]["tile_config_hist"]},
+        "other_modes": out["extra"],
+    }
+    if "e2e" in out:
+        line["e2e"] = out["e2e"]
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

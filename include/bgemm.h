@@ -1,0 +1,164 @@
+/*
+ * bgemm.h -- variable-size batched SGEMM for NVIDIA GB300 (sm_103a).
+ *
+ * C ABI of libbgemm_gb300.so.  Every matrix is column-major:
+ *     C_i <- alpha * A_i * B_i + beta * C_i,   i = 0 .. batch-1
+ * A_i is M_i x K_i (element (m,k) at A_i[m + k*lda_i]), B_i is K_i x N_i
+ * ((k,n) at B_i[k + n*ldb_i]), C_i is M_i x N_i ((m,n) at C_i[m + n*ldc_i]).
+ *
+ * Reference interface replaced (paths inside the BatchGEMM project):
+ *   - the framework kernel entry
+ *       __global__ void gemm(int M[], int N[], int K[], float *A[], float *B[],
+ *                            float *C[], int T_strategy[])
+ *     (CUDA/framework/kernel.h:11), which computes C_i += A_i*B_i over device
+ *     arrays of sizes and pointers, and
+ *   - the host driver that reads the per-matrix sizes, picks a tile strategy
+ *     per matrix, uploads the descriptors and launches one kernel for the
+ *     whole batch (CUDA/framework/gemm.cu:31-77, 88-174, 181-209).
+ * Generalised to the magma-style "vbatched" contract: per-matrix leading
+ * dimensions, alpha/beta, a stream, and status codes instead of exit().
+ *
+ * Numerics of BGEMM_MODE_SIMT_FP32 (bit-exact contract): every output element
+ * is one FP32 fma chain over k = 0..K-1 in order.  When alpha == 1 and
+ * beta == 1 the chain starts from the old C value, exactly like the
+ * reference's tile bodies (C += A*B); otherwise it starts from 0 and the
+ * result is alpha*acc (beta == 0, C is then never read) or
+ * fmaf(alpha, acc, beta*C).
+ *
+ * The tensor-core modes run on tcgen05 with FP32 accumulation in tensor
+ * memory: TF32 (one product of TF32-rounded operands), TF32X3 (hi*hi +
+ * hi*lo + lo*hi of a TF32 hi/lo split) and BF16X3 (the same with a bfloat16
+ * split).  They are checked against an FP64 oracle with a sqrt(K)-scaled
+ * relative tolerance.
+ *
+ * Ownership: the caller owns every A/B/C buffer and the device arrays of
+ * device pointers dA/dB/dC; the library owns its plans, their device
+ * descriptors and workspace.  All device work is asynchronous on `stream`.
+ * A plan may be executed on one stream at a time (its tile queue counter is
+ * reset by the kernel itself at the end of each launch).
+ */
+#ifndef BGEMM_GB300_H
+#define BGEMM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same type as cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st* bgemm_stream_t;
+
+typedef enum bgemm_status {
+  BGEMM_SUCCESS = 0,
+  BGEMM_ERROR_INVALID_VALUE = 1,  /* bgemm_last_error_arg() gives the argument */
+  BGEMM_ERROR_NOT_SUPPORTED = 2,  /* no sm_103 device, or a size beyond a limit */
+  BGEMM_ERROR_ALLOC = 3,          /* device or pinned host allocation failed */
+  BGEMM_ERROR_CUDA = 4,           /* a CUDA runtime call failed */
+  BGEMM_ERROR_DEVICE_TIMEOUT = 5, /* a bounded device-side wait expired; the
+                                     kernel returned early, results invalid */
+  BGEMM_ERROR_INTERNAL = 6
+} bgemm_status_t;
+
+typedef enum bgemm_mode {
+  BGEMM_MODE_SIMT_FP32 = 0, /* FP32 SIMT fma, bit-exact with the reference chain */
+  BGEMM_MODE_TF32 = 1,      /* tcgen05 kind::tf32, one product            */
+  BGEMM_MODE_TF32X3 = 2,    /* tcgen05 kind::tf32, 3-product split (hi/lo) */
+  BGEMM_MODE_BF16X3 = 3     /* tcgen05 kind::f16 (bf16), 3-product split    */
+} bgemm_mode_t;
+
+typedef struct bgemm_plan_s* bgemm_plan_t;
+
+/* Per-plan facts (for benchmarks and tests). */
+typedef struct bgemm_plan_info {
+  int batch;
+  int mode;
+  int num_tiles;            /* work items in the largest-first tile queue   */
+  int grid;                 /* persistent CTAs launched per execute          */
+  int tile_config_hist[16]; /* matrices per tile configuration               */
+  double useful_flops;      /* sum 2*M*N*K                                    */
+  double min_bytes;         /* compulsory HBM bytes: 4*(MK + KN + MN(1 + [beta!=0])) at beta=0 */
+  size_t device_bytes;      /* descriptors + queue + workspace owned by the plan */
+  size_t workspace_bytes;   /* split-operand workspace (tensor-core modes)   */
+} bgemm_plan_info_t;
+
+/* Options for bgemm_plan_create_ex (zero-initialise, then set fields). */
+typedef struct bgemm_plan_options {
+  int force_tile_config;    /* -1: heuristic; otherwise a config id of the mode */
+  int max_ctas;             /* 0: one wave of persistent CTAs; otherwise a cap  */
+  int disable_rebalance;    /* 1: skip the parallelism (wavefront) rebalance    */
+  int reserved[8];
+} bgemm_plan_options_t;
+
+/* --- one-shot entry (host size arrays, like CUDA/framework/gemm.cu:39-41) ---
+ * M, N, K, lda, ldb, ldc: HOST arrays [batch]; dA, dB, dC: DEVICE arrays
+ * [batch] of device pointers.  Requirements: M,N,K >= 0, lda >= max(1,M),
+ * ldb >= max(1,K), ldc >= max(1,M); pointers of empty matrices are not read.
+ * Plans are cached per (shapes, mode, stream); a cache miss builds and
+ * uploads a plan on `stream` without blocking on the GPU. */
+bgemm_status_t bgemm_sgemm_vbatched(const int* M, const int* N, const int* K,
+                                    float alpha, const float* const* dA,
+                                    const int* lda, const float* const* dB,
+                                    const int* ldb, float beta,
+                                    float* const* dC, const int* ldc,
+                                    int batch, bgemm_mode_t mode,
+                                    bgemm_stream_t stream);
+
+/* --- plan / execute split (execute allocates nothing: capturable) --------- */
+bgemm_status_t bgemm_plan_create(bgemm_plan_t* plan, const int* M,
+                                 const int* N, const int* K, const int* lda,
+                                 const int* ldb, const int* ldc, int batch,
+                                 bgemm_mode_t mode, bgemm_stream_t stream);
+bgemm_status_t bgemm_plan_create_ex(bgemm_plan_t* plan, const int* M,
+                                    const int* N, const int* K,
+                                    const int* lda, const int* ldb,
+                                    const int* ldc, int batch,
+                                    bgemm_mode_t mode, bgemm_stream_t stream,
+                                    const bgemm_plan_options_t* options);
+bgemm_status_t bgemm_plan_execute(bgemm_plan_t plan, float alpha,
+                                  const float* const* dA,
+                                  const float* const* dB, float beta,
+                                  float* const* dC, bgemm_stream_t stream);
+bgemm_status_t bgemm_plan_info(bgemm_plan_t plan, bgemm_plan_info_t* info);
+/* Blocks until the plan's previous launches on `stream` finish and reports
+ * BGEMM_ERROR_DEVICE_TIMEOUT if a device-side wait expired in any of them
+ * (the flag is then cleared). */
+bgemm_status_t bgemm_plan_check_device(bgemm_plan_t plan, bgemm_stream_t stream);
+bgemm_status_t bgemm_plan_destroy(bgemm_plan_t plan);
+
+/* --- reference drop-in: the framework kernel's own argument list ----------
+ * Device arrays dM, dN, dK [batch] and dA, dB, dC [batch] exactly as the
+ * reference passes them to gemm<<<...>>>(M, N, K, A, B, C, T_strategy)
+ * (CUDA/framework/gemm.cu:200, kernel.h:11); computes C_i += A_i*B_i with
+ * lda = M_i, ldb = K_i, ldc = M_i in FP32 SIMT (the reference's in-place
+ * fma chain, bit-exact).  dT (the reference's per-matrix tile strategy) may
+ * be NULL; it is ignored because this library picks tiles itself.  Sizes
+ * never leave the device: a device-side pass builds the tile queue, so the
+ * call needs no host copy of M/N/K.  max_dim bounds every M_i and N_i (the
+ * queue capacity is sized from it); M_i or N_i above it is an error reported
+ * by bgemm_framework_check_device(). */
+bgemm_status_t bgemm_framework_gemm(const int* dM, const int* dN,
+                                    const int* dK, float* const* dA,
+                                    float* const* dB, float* const* dC,
+                                    const int* dT, int batch, int max_dim,
+                                    bgemm_stream_t stream);
+bgemm_status_t bgemm_framework_check_device(bgemm_stream_t stream);
+
+/* --- errors and device facts --------------------------------------------- */
+/* 1-based position of the first invalid argument of the last failing call on
+ * this host thread (BLAS convention), 0 if none; for per-matrix arrays the
+ * offending matrix index is returned through *matrix (may be NULL). */
+int bgemm_last_error_arg(int* matrix);
+const char* bgemm_last_error_message(void);
+const char* bgemm_status_string(bgemm_status_t status);
+/* Number of SMs of the current device and persistent CTAs per SM per mode. */
+bgemm_status_t bgemm_device_info(int* num_sms, int* simt_ctas_per_sm,
+                                 int* tc_ctas_per_sm);
+/* Library version, e.g. 100 for 0.1.0. */
+int bgemm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BGEMM_GB300_H */

@@ -1,0 +1,31 @@
+/*
+ * bgemm_debug.h -- host-only introspection of libbgemm_gb300.so's planner,
+ * for tests and the autotuner.  Needs no GPU.
+ *
+ * Replaces the reference's host tile-strategy pass (CUDA/framework/gemm.cu:
+ * 107-169, the per-matrix T_strategy choice and the wavefront demotion loop)
+ * as an observable function: given the sizes and the number of persistent
+ * CTA slots, it returns each matrix's tile configuration and the ordered
+ * tile queue the SIMT kernel would pull.
+ */
+#ifndef BGEMM_GB300_DEBUG_H
+#define BGEMM_GB300_DEBUG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cfg_out [batch] receives the SIMT tile configuration of each matrix (-1 for
+ * empty matrices); items_out [3*max_items] receives (matrix, tile_m, tile_n)
+ * per queue slot in pull order (may be NULL to only count).  force_cfg < 0
+ * lets the heuristic choose; rebalance != 0 enables the parallelism
+ * rebalance for `slots` persistent CTAs.  Returns the number of work items,
+ * or -1 on invalid sizes or when max_items is too small. */
+int bgemm_debug_simt_queue(const int* M, const int* N, const int* K, int batch, int slots,
+                           int force_cfg, int rebalance, int* cfg_out, int* items_out,
+                           int max_items);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
