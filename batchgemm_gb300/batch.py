@@ -110,10 +110,14 @@ class DeviceBatch:
         return self
 
     def set_from_numpy(self, As, Bs, Cs) -> "DeviceBatch":
+        """Copies in matrices given as 2-D arrays or flat column-major (ld = rows) data."""
         for i in range(self.batch):
             for v, arr in ((self.a(i), As[i]), (self.b(i), Bs[i]), (self.c(i), Cs[i])):
                 if v.numel():
-                    v.copy_(torch.from_numpy(np.asarray(arr, np.float32)).to(self.device))
+                    a = np.asarray(arr, np.float32)
+                    if a.ndim == 1:
+                        a = a.reshape(v.shape[1], v.shape[0]).T
+                    v.copy_(torch.from_numpy(np.ascontiguousarray(a)).to(self.device))
         return self
 
     # -- running ----------------------------------------------------------
