@@ -45,6 +45,7 @@ class PlanInfo(ctypes.Structure):
         ("grid", ctypes.c_int), ("tile_config_hist", ctypes.c_int * 16),
         ("useful_flops", ctypes.c_double), ("min_bytes", ctypes.c_double),
         ("device_bytes", ctypes.c_size_t), ("workspace_bytes", ctypes.c_size_t),
+        ("kernels_per_execute", ctypes.c_int), ("reserved", ctypes.c_int * 7),
     ]
 
     def as_dict(self):
@@ -53,6 +54,7 @@ class PlanInfo(ctypes.Structure):
             "grid": self.grid, "tile_config_hist": list(self.tile_config_hist),
             "useful_flops": self.useful_flops, "min_bytes": self.min_bytes,
             "device_bytes": self.device_bytes, "workspace_bytes": self.workspace_bytes,
+            "kernels_per_execute": self.kernels_per_execute,
         }
 
 

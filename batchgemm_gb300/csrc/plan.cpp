@@ -91,14 +91,22 @@ bgemm_status_t device_facts(DeviceFacts* out) {
 static inline long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
 
 // Candidate (cost, tiles) of configuration c for matrix (M, N, K).
-static inline void simt_eval(int c, int M, int N, int K, long long* tiles, double* t_tile) {
+static bool simt_eval(int c, int M, int N, int K, long long* tiles, double* t_tile) {
   const SimtCfg& g = kSimtCfgs[c];
+  if (ceil_div(M, g.bm) > 65535 || ceil_div(N, g.bn) > 65535) return false;
   *tiles = ceil_div(M, g.bm) * ceil_div(N, g.bn);
   *t_tile = kSimtCost[c].a_ns + kSimtCost[c].b_ns * (double)K;
+  return true;
 }
 
 static bgemm_status_t choose_simt(const int* M, const int* N, const int* K, int batch, int slots,
                                   const bgemm_plan_options_t* opt, std::vector<MatPlan>& mp) {
+  return choose_tiles(kSimtNumCfgs, simt_eval, M, N, K, batch, slots, opt, mp);
+}
+
+bgemm_status_t choose_tiles(int ncfg, TileEval eval, const int* M, const int* N, const int* K,
+                            int batch, int slots, const bgemm_plan_options_t* opt,
+                            std::vector<MatPlan>& mp) {
   mp.assign(batch, MatPlan{-1, 0, 0.0});
   double total = 0.0;
   for (int i = 0; i < batch; ++i) {
@@ -106,19 +114,19 @@ static bgemm_status_t choose_simt(const int* M, const int* N, const int* K, int 
     int best = -1;
     long long bt = 0;
     double bw = 0, btt = 0;
-    for (int c = kSimtNumCfgs - 1; c >= 0; --c) {
+    for (int c = ncfg - 1; c >= 0; --c) {
       if (opt && opt->force_tile_config >= 0 && c != opt->force_tile_config) continue;
       long long t;
       double tt;
-      simt_eval(c, M[i], N[i], K[i], &t, &tt);
+      if (!eval(c, M[i], N[i], K[i], &t, &tt)) continue;
       const double w = (double)t * tt;
       if (best < 0 || w < bw * 0.999) {
         best = c; bt = t; bw = w; btt = tt;
       }
     }
-    if (bt > 65535LL * 65535LL || ceil_div(M[i], kSimtCfgs[best].bm) > 65535 ||
-        ceil_div(N[i], kSimtCfgs[best].bn) > 65535)
-      return set_error(BGEMM_ERROR_NOT_SUPPORTED, 1, i, "matrix %d: too many tiles", i);
+    if (best < 0 || bt > (1LL << 31))
+      return set_error(BGEMM_ERROR_NOT_SUPPORTED, 1, i, "matrix %d: no tile configuration fits",
+                       i);
     mp[i] = MatPlan{best, bt, btt};
     total += bw;
   }
@@ -140,10 +148,10 @@ static bgemm_status_t choose_simt(const int* M, const int* N, const int* K, int 
     int best = -1;
     long long bt = 0;
     double btt = 0, bw = 0;
-    for (int c = 0; c < kSimtNumCfgs; ++c) {
+    for (int c = 0; c < ncfg; ++c) {
       long long t;
       double t2;
-      simt_eval(c, M[i], N[i], K[i], &t, &t2);
+      if (!eval(c, M[i], N[i], K[i], &t, &t2)) continue;
       if (t2 >= tt || t <= mp[i].tiles) continue;
       const double w = (double)t * t2;
       if (best < 0 || w < bw) { best = c; bt = t; btt = t2; bw = w; }
@@ -294,6 +302,7 @@ bgemm_status_t plan_create(bgemm_plan_t* out, const int* M, const int* N, const 
     st = tc_choose(p, M, N, K, batch, opt, mp);
   }
   if (st != BGEMM_SUCCESS) {
+    free_plan_memory(p);
     delete p;
     return st;
   }
@@ -340,6 +349,8 @@ bgemm_status_t plan_create(bgemm_plan_t* out, const int* M, const int* N, const 
     if (mp[i].cfg >= 0 && mp[i].cfg < 16) p->info.tile_config_hist[mp[i].cfg]++;
   }
   expand_items(mode, p, M, N, mp, order, hd, hi);
+  p->host_descs.assign(hd, hd + batch);
+  p->info.kernels_per_execute = (mode == BGEMM_MODE_SIMT_FP32) ? 1 : 2;
   p->d_counters = reinterpret_cast<int*>(static_cast<char*>(p->d_mem));
   p->d_descs = reinterpret_cast<MatDesc*>(static_cast<char*>(p->d_mem) + off_desc);
   p->d_items = reinterpret_cast<TileItem*>(static_cast<char*>(p->d_mem) + off_items);

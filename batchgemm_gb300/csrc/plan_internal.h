@@ -43,6 +43,7 @@ struct bgemm_plan_s {
   bgemm::TileItem* d_items = nullptr;
   char* d_extra = nullptr;
   bgemm::TcPlan* tc = nullptr;
+  std::vector<bgemm::MatDesc> host_descs;
   bgemm_plan_info_t info{};
 };
 
@@ -51,6 +52,15 @@ namespace bgemm {
 bgemm_status_t set_error(bgemm_status_t st, int arg, int mat, const char* fmt, ...);
 bgemm_status_t cuda_error(cudaError_t e, const char* what);
 bgemm_status_t device_facts(DeviceFacts* out);
+
+// Tile count and modelled time of one tile of configuration c; false if the
+// configuration cannot take the matrix.
+using TileEval = bool (*)(int c, int M, int N, int K, long long* tiles, double* t_tile);
+// Per-matrix least-total-time choice, then the parallelism rebalance over
+// `slots` persistent CTAs (shared by the SIMT and tensor-core planners).
+bgemm_status_t choose_tiles(int ncfg, TileEval eval, const int* M, const int* N, const int* K,
+                            int batch, int slots, const bgemm_plan_options_t* opt,
+                            std::vector<MatPlan>& mp);
 
 // tensor-core hooks (tc_plan.cpp)
 bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int* K, int batch,

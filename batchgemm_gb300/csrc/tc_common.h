@@ -1,0 +1,68 @@
+// tc_common.h -- structures of the tensor-core (tcgen05) path shared by the
+// planner and the kernels.
+#pragma once
+#include <stdint.h>
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "bgemm_internal.h"
+
+namespace bgemm {
+
+// Element kinds of the packed operands.
+enum TcKind : int { kKindTF32 = 0, kKindBF16 = 1 };
+
+// Tile configurations: UMMA M = 128 rows of the "A side" operand, UMMA N =
+// BN rows of the "B side".  Ids 0..3 keep A on the A side (BN 16/32/64/128);
+// ids 4..7 swap the operands (C^T = B^T A^T, the A side walks N) for
+// matrices whose M is small.
+constexpr int kTcBM = 128;
+constexpr int kTcMaxBN = 128;
+__host__ __device__ constexpr int tc_cfg_bn(int cfg) { return 16 << (cfg & 3); }
+__host__ __device__ constexpr bool tc_cfg_swap(int cfg) { return (cfg & 4) != 0; }
+
+// One pre-pass job: split/pack a strip of 32 rows of one operand.
+struct PackJob {
+  int mat;
+  int op;  // 0: A (M x K, transposed to rows of K), 1: B (N x K rows)
+  int r0;  // first row of the strip
+  int pad;
+};
+
+// Where the packed operands of a matrix live (byte offsets into the workspace).
+struct PackDesc {
+  long long a_hi, a_lo, b_hi, b_lo;
+  int kpad;  // row length in elements (K rounded up to 16 bytes)
+  int pad[3];
+};
+
+struct TcPackParams {
+  const MatDesc* descs;
+  const PackDesc* pdescs;
+  const PackJob* jobs;
+  int n_jobs;
+  int kind;
+  int split;
+  char* ws;
+  const float* const* A;
+  const float* const* B;
+};
+
+struct TcGemmParams {
+  const MatDesc* descs;
+  const TileItem* items;
+  int n_items;
+  int* counters;               // [0] queue head, [1] CTAs finished
+  const CUtensorMap* tmaps;    // 4 per matrix: A-side hi, A-side lo, B-side hi, B-side lo
+  float alpha, beta;
+  float* const* C;
+  int* error;                  // bit 0: a bounded device wait expired
+  unsigned long long timeout_ns;
+};
+
+cudaError_t tc_pack_launch(const TcPackParams& p, int grid, cudaStream_t s);
+cudaError_t tc_gemm_launch(int kind, int split, const TcGemmParams& p, int grid, cudaStream_t s);
+int tc_smem_bytes(int kind, int split);
+
+}  // namespace bgemm

@@ -1,0 +1,539 @@
+// tc_kernel.cu -- tensor-core (tcgen05 / TMEM) form of the variable-size
+// batched SGEMM for sm_103a.
+//
+// Two kernels per execute:
+//   tc_pack_kernel  splits every operand element x into hi = round(x) and
+//                   lo = round(x - hi) (TF32 or BF16, round to nearest even)
+//                   and writes them K-major ("rows of K", 16-byte aligned row
+//                   length) into the plan's workspace: A is transposed from
+//                   column-major M x K, B (column-major K x N) is already
+//                   K-major.  Ragged edges of any shape and leading dimension
+//                   are handled here, so the GEMM sees only TMA-legal tiles.
+//   tc_gemm_kernel  one persistent CTA per SM pulls output tiles from the
+//                   largest-first queue.  Warp 0 (one lane) is the TMA
+//                   producer and tile scheduler, warp 1 (one lane) issues
+//                   tcgen05.mma into a double-buffered TMEM accumulator,
+//                   warps 2-5 drain TMEM (tcgen05.ld), apply alpha/beta and
+//                   store C.  Per 128-byte K slice a stage holds the hi (and
+//                   lo) tiles of both sides, TMA-loaded with 128-byte swizzle
+//                   through per-matrix tensor maps.
+// Split modes keep hi*hi in one TMEM accumulator and hi*lo + lo*hi in a
+// second, added in FP32 at the end, so the small terms are not rounded
+// against the large partial sums.
+//
+// Every wait on an mbarrier is bounded (global timer); on expiry the kernel
+// sets an error flag, lets in-flight copies and MMAs land, frees TMEM and
+// returns, and the host reports BGEMM_ERROR_DEVICE_TIMEOUT.
+//
+// Reference counterpart: the reference's FP32 tile bodies
+// (CUDA/framework/kernel_128_new.h, kernel_256_new.h) have no tensor-core
+// form; this file is the new precision path that the tile queue drives.
+#include <stdint.h>
+
+#include "tc_common.h"
+
+namespace bgemm {
+namespace {
+
+constexpr int kABytes = kTcBM * 128;        // 128 rows x 128 bytes of K
+constexpr int kBBytes = kTcMaxBN * 128;     // up to 128 rows x 128 bytes
+constexpr int kSchedSlots = 4;
+constexpr int kThreads = 192;
+
+template <int SPLIT>
+struct Geo {
+  static constexpr int NP = SPLIT ? 2 : 1;
+  static constexpr int STAGE = (kABytes + kBBytes) * NP;
+  static constexpr int S = SPLIT ? 3 : 6;
+  static constexpr int NBAR = 2 * S + 2 * kSchedSlots + 4 + 1;
+  static constexpr int BYTES = S * STAGE + NBAR * 8 + kSchedSlots * 4 + 16 + 1024;
+};
+
+// ------------------------------------------------------------- PTX glue --
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint64_t gtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t a, uint32_t tx) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(tx)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void prefetch_tmap(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+template <int KIND>
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                    uint32_t accumulate) {
+  if constexpr (KIND == kKindTF32) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+  } else {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+  }
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major tile written by TMA with
+// 128-byte swizzle: 8-row x 128-byte atoms, 1024 bytes apart (SBO); the
+// leading offset is unused for this layout (encoded as 1); version 1;
+// layout type 2 = SWIZZLE_128B.  Advancing along K inside the atom is a
+// plain add to the start address (the swizzle is applied on address bits).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1u << 16) | ((uint64_t)(1024u >> 4) << 32) |
+         ((uint64_t)1u << 46) | ((uint64_t)2u << 61);
+}
+
+// Instruction descriptor: D = F32 (bits 4-5 = 1), A/B format (bits 7-9,
+// 10-12: TF32 = 2 for kind::tf32, BF16 = 1 for kind::f16), both K-major,
+// N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+template <int KIND>
+__device__ __forceinline__ uint32_t make_idesc(int n) {
+  constexpr uint32_t fmt = (KIND == kKindTF32) ? 2u : 1u;
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(kTcBM >> 4) << 24);
+}
+
+struct Ring {
+  uint32_t idx = 0, phase = 0;
+  __device__ __forceinline__ void next(uint32_t n) {
+    if (++idx == n) {
+      idx = 0;
+      phase ^= 1u;
+    }
+  }
+};
+
+// Bounded wait; returns false if the wait expired (error flag set) or
+// another role already aborted.
+__device__ __noinline__ bool wait_bounded(uint32_t bar, uint32_t parity, int* err,
+                                          volatile int* abort, unsigned long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = gtimer();
+  for (uint32_t i = 1;; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63u) == 0) {
+      if (abort && *abort) return false;
+      if (gtimer() - t0 > limit_ns) {
+        atomicOr(err, 1);
+        if (abort) *abort = 1;
+        return false;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------- operand splitting --
+__device__ __forceinline__ float round_keep(float x, int drop) {
+  uint32_t u = __float_as_uint(x);
+  if ((u & 0x7f800000u) == 0x7f800000u) return x;
+  const uint32_t half = (1u << (drop - 1)) - 1u;
+  u += half + ((u >> drop) & 1u);
+  u &= ~((1u << drop) - 1u);
+  return __uint_as_float(u);
+}
+
+__device__ __forceinline__ void put(char* hi, char* lo, long long idx, float x, int kind,
+                                    int split) {
+  if (kind == kKindTF32) {
+    const float h = round_keep(x, 13);
+    reinterpret_cast<float*>(hi)[idx] = h;
+    if (split) {
+      const bool fin = (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u;
+      reinterpret_cast<float*>(lo)[idx] = fin ? round_keep(x - h, 13) : 0.0f;
+    }
+  } else {
+    const float h = round_keep(x, 16);
+    reinterpret_cast<uint16_t*>(hi)[idx] = (uint16_t)(__float_as_uint(h) >> 16);
+    if (split) {
+      const bool fin = (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u;
+      const float l = fin ? round_keep(x - h, 16) : 0.0f;
+      reinterpret_cast<uint16_t*>(lo)[idx] = (uint16_t)(__float_as_uint(l) >> 16);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
+  __shared__ float t[32][33];
+  for (int j = blockIdx.x; j < p.n_jobs; j += gridDim.x) {
+    const PackJob job = p.jobs[j];
+    const MatDesc d = p.descs[job.mat];
+    const PackDesc pd = p.pdescs[job.mat];
+    const int K = d.K;
+    const long long kpad = pd.kpad;
+    if (job.op == 0) {
+      const float* A = p.A[job.mat];
+      const long long lda = d.lda;
+      char* hi = p.ws + pd.a_hi;
+      char* lo = p.ws + pd.a_lo;
+      for (int k0 = 0; k0 < K; k0 += 32) {
+        for (int e = threadIdx.x; e < 1024; e += 256) {
+          const int kk = e >> 5, mm = e & 31;
+          const int m = job.r0 + mm, k = k0 + kk;
+          t[kk][mm] = (m < d.M && k < K) ? A[m + k * lda] : 0.0f;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < 1024; e += 256) {
+          const int mm = e >> 5, kk = e & 31;
+          const int m = job.r0 + mm, k = k0 + kk;
+          if (m < d.M && k < K) put(hi, lo, m * kpad + k, t[kk][mm], p.kind, p.split);
+        }
+        __syncthreads();
+      }
+    } else {
+      const float* B = p.B[job.mat];
+      const long long ldb = d.ldb;
+      char* hi = p.ws + pd.b_hi;
+      char* lo = p.ws + pd.b_lo;
+      for (int k0 = 0; k0 < K; k0 += 32) {
+        for (int e = threadIdx.x; e < 1024; e += 256) {
+          const int nn = e >> 5, kk = e & 31;
+          const int n = job.r0 + nn, k = k0 + kk;
+          if (n < d.N && k < K) put(hi, lo, n * kpad + k, B[k + n * ldb], p.kind, p.split);
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------- the GEMM --
+template <int KIND, int SPLIT>
+__global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams p) {
+  using G = Geo<SPLIT>;
+  constexpr int S = G::S;
+  constexpr int KE = (KIND == kKindTF32) ? 32 : 64;  // elements per 128-byte slice
+  constexpr int NSUB = 4;                             // MMAs of 32 bytes of K per slice
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
+  uint8_t* smem = smem_raw + pad;
+  const uint32_t sbase = raw + pad;
+
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * G::STAGE);
+  const uint32_t bar0 = sbase + S * G::STAGE;
+  auto full = [&](int s) { return bar0 + 8u * s; };
+  auto empty = [&](int s) { return bar0 + 8u * (S + s); };
+  auto sfull = [&](int s) { return bar0 + 8u * (2 * S + s); };
+  auto sempty = [&](int s) { return bar0 + 8u * (2 * S + kSchedSlots + s); };
+  auto tfull = [&](int s) { return bar0 + 8u * (2 * S + 2 * kSchedSlots + s); };
+  auto tempty = [&](int s) { return bar0 + 8u * (2 * S + 2 * kSchedSlots + 2 + s); };
+  const uint32_t drain = bar0 + 8u * (2 * S + 2 * kSchedSlots + 4);
+  volatile int* slots = reinterpret_cast<volatile int*>(bars + G::NBAR);
+  volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(slots + kSchedSlots);
+  volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(full(s), 1);
+      mbar_init(empty(s), 1);
+    }
+    for (int s = 0; s < kSchedSlots; ++s) {
+      mbar_init(sfull(s), 1);
+      mbar_init(sempty(s), 1 + 4);
+    }
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(tfull(s), 1);
+      mbar_init(tempty(s), 4);
+    }
+    mbar_init(drain, 1);
+    *abort = 0;
+    fence_mbar_init();
+  }
+  if (warp == 1) {
+    tmem_alloc(smem_u32(const_cast<uint32_t*>(tmem_slot)), 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------ producer + scheduler
+    if (lane == 0) {
+      Ring st, sc;
+      int inflight_phase[S];
+      bool inflight[S];
+      for (int s = 0; s < S; ++s) inflight[s] = false, inflight_phase[s] = 0;
+      int last_mat = -1;
+      for (;;) {
+        const int it = atomicAdd(p.counters, 1);
+        if (!wait_bounded(sempty(sc.idx), sc.phase ^ 1u, p.error, abort, p.timeout_ns)) break;
+        slots[sc.idx] = (it < p.n_items) ? it : -1;
+        mbar_arrive(sfull(sc.idx));
+        sc.next(kSchedSlots);
+        if (it >= p.n_items) break;
+        const TileItem ti = p.items[it];
+        const MatDesc d = p.descs[ti.mat];
+        const int bn = tc_cfg_bn(d.cfg);
+        const CUtensorMap* tm = p.tmaps + 4 * ti.mat;
+        if (ti.mat != last_mat && d.K > 0) {
+          prefetch_tmap(tm);
+          prefetch_tmap(tm + 2);
+          last_mat = ti.mat;
+        }
+        const int nk = (d.K + KE - 1) / KE;
+        const uint32_t tx = (uint32_t)(kABytes + bn * 128) * G::NP;
+        const int row_a = ti.tm * kTcBM;
+        const int row_b = ti.tn * bn;
+        bool ok = true;
+        for (int kb = 0; kb < nk; ++kb) {
+          if (!wait_bounded(empty(st.idx), st.phase ^ 1u, p.error, abort, p.timeout_ns)) {
+            ok = false;
+            break;
+          }
+          const uint32_t sa = sbase + st.idx * G::STAGE;
+          const uint32_t sb = sa + kABytes * G::NP;
+          mbar_arrive_expect_tx(full(st.idx), tx);
+          inflight[st.idx] = true;
+          inflight_phase[st.idx] = st.phase;
+          tma_load_2d(sa, tm + 0, kb * KE, row_a, full(st.idx));
+          tma_load_2d(sb, tm + 2, kb * KE, row_b, full(st.idx));
+          if (SPLIT) {
+            tma_load_2d(sa + kABytes, tm + 1, kb * KE, row_a, full(st.idx));
+            tma_load_2d(sb + kBBytes, tm + 3, kb * KE, row_b, full(st.idx));
+          }
+          st.next(S);
+        }
+        if (!ok) break;
+      }
+      // Let every copy this thread issued land before the CTA can exit.
+      for (int s = 0; s < S; ++s)
+        if (inflight[s])
+          wait_bounded(full(s), (uint32_t)inflight_phase[s], p.error, nullptr, p.timeout_ns);
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ----------------------------------------------------------- MMA issue
+    if (lane == 0) {
+      Ring st, sc, acc;
+      for (;;) {
+        if (!wait_bounded(sfull(sc.idx), sc.phase, p.error, abort, p.timeout_ns)) break;
+        const int it = slots[sc.idx];
+        mbar_arrive(sempty(sc.idx));
+        sc.next(kSchedSlots);
+        if (it < 0) break;
+        const TileItem ti = p.items[it];
+        const MatDesc d = p.descs[ti.mat];
+        const int bn = tc_cfg_bn(d.cfg);
+        const uint32_t idesc = make_idesc<KIND>(bn);
+        const int nk = (d.K + KE - 1) / KE;
+        if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) break;
+        tc_fence_after();
+        const uint32_t d_main = tmem + acc.idx * 256u;
+        const uint32_t d_corr = d_main + 128u;
+        bool ok = true;
+        for (int kb = 0; kb < nk; ++kb) {
+          if (!wait_bounded(full(st.idx), st.phase, p.error, abort, p.timeout_ns)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = sbase + st.idx * G::STAGE;
+          const uint32_t sb = sa + kABytes * G::NP;
+#pragma unroll
+          for (int s = 0; s < NSUB; ++s) {
+            const uint64_t ah = sw128_desc(sa + 32u * s);
+            const uint64_t bh = sw128_desc(sb + 32u * s);
+            const uint32_t accum = (kb > 0 || s > 0) ? 1u : 0u;
+            mma<KIND>(d_main, ah, bh, idesc, accum);
+            if (SPLIT) {
+              const uint64_t al = sw128_desc(sa + kABytes + 32u * s);
+              const uint64_t bl = sw128_desc(sb + kBBytes + 32u * s);
+              mma<KIND>(d_corr, ah, bl, idesc, accum);
+              mma<KIND>(d_corr, al, bh, idesc, 1u);
+            }
+          }
+          mma_commit(empty(st.idx));
+          st.next(S);
+        }
+        if (!ok) break;
+        mma_commit(tfull(acc.idx));
+        acc.next(2);
+      }
+      // all MMAs issued by this thread complete before TMEM is freed
+      mma_commit(drain);
+      wait_bounded(drain, 0, p.error, nullptr, p.timeout_ns);
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int q = warp & 3;  // this warp may read TMEM lanes 32q .. 32q+31
+    Ring sc, acc;
+    const float alpha = p.alpha, beta = p.beta;
+    for (;;) {
+      int ok = 1;
+      if (lane == 0) ok = wait_bounded(sfull(sc.idx), sc.phase, p.error, abort, p.timeout_ns);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      const int it = slots[sc.idx];
+      __syncwarp();
+      if (lane == 0) mbar_arrive(sempty(sc.idx));
+      sc.next(kSchedSlots);
+      if (it < 0) break;
+      const TileItem ti = p.items[it];
+      const MatDesc d = p.descs[ti.mat];
+      float* C = p.C[ti.mat];
+      const int bn = tc_cfg_bn(d.cfg);
+      const bool swap = tc_cfg_swap(d.cfg);
+      if (lane == 0) ok = wait_bounded(tfull(acc.idx), acc.phase, p.error, abort, p.timeout_ns);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      tc_fence_after();
+      const int row = ti.tm * kTcBM + q * 32 + lane;  // A-side row
+      const long long ldc = d.ldc;
+      const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + acc.idx * 256u;
+      const bool kzero = d.K == 0;
+      for (int c0 = 0; c0 < bn; c0 += 16) {
+        float v[16], u[16];
+        tmem_ld16(tb + c0, v);
+        if (SPLIT) tmem_ld16(tb + 128u + c0, u);
+        tmem_wait_ld();
+        const int col0 = ti.tn * bn + c0;  // B-side index of v[0]
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          float x = SPLIT ? v[j] + u[j] : v[j];
+          if (kzero) x = 0.0f;
+          const int m = swap ? col0 + j : row;
+          const int n = swap ? row : col0 + j;
+          if (m < d.M && n < d.N) {
+            float* c = C + m + n * ldc;
+            *c = (beta == 0.0f) ? alpha * x : fmaf(alpha, x, beta * *c);
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tempty(acc.idx));
+      acc.next(2);
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc(tmem, 512);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(reinterpret_cast<unsigned*>(p.counters) + 1, 1u);
+    if (prev == gridDim.x - 1) {
+      atomicExch(p.counters, 0);
+      atomicExch(p.counters + 1, 0);
+      __threadfence();
+    }
+  }
+}
+
+template <int KIND, int SPLIT>
+cudaError_t launch_gemm(const TcGemmParams& p, int grid, cudaStream_t s) {
+  static bool attr = false;
+  const int bytes = Geo<SPLIT>::BYTES;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<KIND, SPLIT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  tc_gemm_kernel<KIND, SPLIT><<<grid, kThreads, bytes, s>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t tc_pack_launch(const TcPackParams& p, int grid, cudaStream_t s) {
+  if (p.n_jobs == 0) return cudaSuccess;
+  tc_pack_kernel<<<grid, 256, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t tc_gemm_launch(int kind, int split, const TcGemmParams& p, int grid, cudaStream_t s) {
+  if (kind == kKindTF32 && !split) return launch_gemm<kKindTF32, 0>(p, grid, s);
+  if (kind == kKindTF32 && split) return launch_gemm<kKindTF32, 1>(p, grid, s);
+  if (kind == kKindBF16 && split) return launch_gemm<kKindBF16, 1>(p, grid, s);
+  return cudaErrorInvalidValue;
+}
+
+int tc_smem_bytes(int kind, int split) {
+  (void)kind;
+  return split ? Geo<1>::BYTES : Geo<0>::BYTES;
+}
+
+}  // namespace bgemm

@@ -1,24 +1,241 @@
-// tc_plan.cpp -- planner hooks of the tensor-core modes (placeholder until
-// the tcgen05 kernel lands).
+// tc_plan.cpp -- planner of the tensor-core modes: per-matrix tile
+// configuration (orientation and MMA width), split-operand workspace layout,
+// pack jobs, per-matrix TMA tensor maps, and the two launches of an execute.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include <cudaTypedefs.h>
+
 #include "plan_internal.h"
+#include "tc_common.h"
 
 namespace bgemm {
 
-bgemm_status_t tc_choose(bgemm_plan_s*, const int*, const int*, const int*, int,
-                         const bgemm_plan_options_t*, std::vector<MatPlan>&) {
-  return set_error(BGEMM_ERROR_NOT_SUPPORTED, 13, -1, "tensor-core modes are not built yet");
+struct TcPlan {
+  int kind = kKindTF32;
+  int split = 1;
+  int nprod = 3;
+  void* d_ws = nullptr;      // split operands
+  size_t ws_bytes = 0;
+  void* d_mem = nullptr;     // tensor maps | pack descs | jobs | error word
+  void* h_pin = nullptr;
+  CUtensorMap* d_tmaps = nullptr;
+  PackDesc* d_pdescs = nullptr;
+  PackJob* d_jobs = nullptr;
+  int* d_err = nullptr;
+  int n_jobs = 0;
+  int pack_grid = 1;
+};
+
+static inline long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
+
+// tensor-pipe rate of one SM, flops per ns (TF32: 4096 flops/clk at ~1.9 GHz)
+static double g_rate_ns = 7782.0;
+static int g_nprod = 3;
+static int g_kind = kKindTF32;
+
+// Modelled tile time: a fixed part plus the MMA time of K, where MMAs
+// narrower than 64 columns cost as much as 64 (operand reads dominate).
+static bool tc_eval(int c, int M, int N, int K, long long* tiles, double* t_tile) {
+  const bool swap = tc_cfg_swap(c);
+  const int bn = tc_cfg_bn(c);
+  const long long ra = swap ? N : M, rb = swap ? M : N;
+  if (cdiv(ra, kTcBM) > 65535 || cdiv(rb, bn) > 65535) return false;
+  *tiles = cdiv(ra, kTcBM) * cdiv(rb, bn);
+  const double rate = g_rate_ns * (g_kind == kKindBF16 ? 2.0 : 1.0);
+  *t_tile = 1200.0 + 2.0 * kTcBM * std::max(bn, 64) * g_nprod * (double)K / rate;
+  return true;
 }
-void tc_tile_dims(bgemm_plan_s*, int, int, int, int, int* bm, int* bn, MatDesc*) {
-  *bm = 128;
-  *bn = 128;
+
+bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int* K, int batch,
+                         const bgemm_plan_options_t* opt, std::vector<MatPlan>& mp) {
+  auto* t = new TcPlan();
+  t->kind = (p->mode == BGEMM_MODE_BF16X3) ? kKindBF16 : kKindTF32;
+  t->split = (p->mode == BGEMM_MODE_TF32) ? 0 : 1;
+  t->nprod = t->split ? 3 : 1;
+  p->tc = t;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
+  g_nprod = t->nprod;
+  g_kind = t->kind;
+  const int slots = p->facts.num_sms * p->facts.tc_ctas_per_sm;
+  return choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, slots, opt, mp);
 }
+
+void tc_tile_dims(bgemm_plan_s*, int, int, int, int cfg, int* bm, int* bn, MatDesc* d) {
+  *bm = kTcBM;
+  *bn = tc_cfg_bn(cfg);
+  d->aux = tc_cfg_swap(cfg) ? kTcSwapFlag : 0;
+}
+
 size_t tc_extra_bytes(bgemm_plan_s*, int) { return 0; }
-bgemm_status_t tc_plan_finish(bgemm_plan_s*, cudaStream_t) { return BGEMM_ERROR_NOT_SUPPORTED; }
-bgemm_status_t tc_execute(bgemm_plan_s*, float, const float* const*, const float* const*, float,
-                          float* const*, cudaStream_t) {
-  return BGEMM_ERROR_NOT_SUPPORTED;
+
+// ----------------------------------------------------------- tensor maps --
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  });
+  return fn;
 }
-bgemm_status_t tc_check_device(bgemm_plan_s*, cudaStream_t) { return BGEMM_SUCCESS; }
-void tc_plan_release(bgemm_plan_s*) {}
+
+// 2-D K-major panel: dim 0 = K (elements, contiguous), dim 1 = rows.
+static bool encode_panel(CUtensorMap* out, int kind, void* base, int K, int rows, int kpad,
+                         int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  const int esz = (kind == kKindTF32) ? 4 : 2;
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)kpad * esz};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(out, kind == kKindTF32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                         : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                  2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream) {
+  TcPlan* t = p->tc;
+  const int batch = p->batch;
+  const int esz = (t->kind == kKindTF32) ? 4 : 2;
+  const int parts = t->split ? 2 : 1;
+  const std::vector<MatDesc>& hd = p->host_descs;
+
+  // workspace layout: per matrix [A hi][A lo][B hi][B lo], rows of kpad
+  std::vector<PackDesc> pd(batch);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += (bytes + 255) & ~size_t(255);
+    return (long long)o;
+  };
+  for (int i = 0; i < batch; ++i) {
+    const MatDesc& d = hd[i];
+    PackDesc& q = pd[i];
+    std::memset(&q, 0, sizeof(q));
+    q.kpad = (int)((d.K + (16 / esz) - 1) / (16 / esz) * (16 / esz));
+    if (d.M == 0 || d.N == 0 || d.K == 0) continue;
+    const size_t a = (size_t)d.M * q.kpad * esz, b = (size_t)d.N * q.kpad * esz;
+    q.a_hi = take(a);
+    q.a_lo = t->split ? take(a) : q.a_hi;
+    q.b_hi = take(b);
+    q.b_lo = t->split ? take(b) : q.b_hi;
+  }
+  t->ws_bytes = std::max<size_t>(off, 256);
+  (void)parts;
+
+  // pack jobs: strips of 32 rows, matrices with the longest K first
+  std::vector<int> order;
+  for (int i = 0; i < batch; ++i)
+    if (hd[i].M > 0 && hd[i].N > 0 && hd[i].K > 0) order.push_back(i);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hd[a].K > hd[b].K; });
+  std::vector<PackJob> jobs;
+  for (int i : order) {
+    for (int r = 0; r < hd[i].M; r += 32) jobs.push_back(PackJob{i, 0, r, 0});
+    for (int r = 0; r < hd[i].N; r += 32) jobs.push_back(PackJob{i, 1, r, 0});
+  }
+  t->n_jobs = (int)jobs.size();
+  t->pack_grid = (int)std::max<long long>(1, std::min<long long>(t->n_jobs,
+                                                                 (long long)p->facts.num_sms * 8));
+
+  const size_t off_tm = 0;
+  const size_t off_pd = off_tm + sizeof(CUtensorMap) * 4 * (size_t)batch;
+  const size_t off_jobs = off_pd + ((sizeof(PackDesc) * (size_t)batch + 255) & ~size_t(255));
+  const size_t off_err = off_jobs + ((sizeof(PackJob) * jobs.size() + 255) & ~size_t(255));
+  const size_t total = off_err + 256;
+
+  cudaError_t e = cudaMalloc(&t->d_ws, t->ws_bytes);
+  if (e != cudaSuccess)
+    return set_error(BGEMM_ERROR_ALLOC, 0, -1, "split-operand workspace of %zu bytes: %s",
+                     t->ws_bytes, cudaGetErrorString(e));
+  e = cudaMalloc(&t->d_mem, total);
+  if (e == cudaSuccess) e = cudaMallocHost(&t->h_pin, total);
+  if (e != cudaSuccess)
+    return set_error(BGEMM_ERROR_ALLOC, 0, -1, "tensor-core plan memory: %s",
+                     cudaGetErrorString(e));
+  char* h = static_cast<char*>(t->h_pin);
+  std::memset(h, 0, total);
+  auto* tm = reinterpret_cast<CUtensorMap*>(h + off_tm);
+  char* ws = static_cast<char*>(t->d_ws);
+  for (int i = 0; i < batch; ++i) {
+    const MatDesc& d = hd[i];
+    if (d.M == 0 || d.N == 0 || d.K == 0) continue;
+    const bool swap = tc_cfg_swap(d.cfg);
+    const int bn = tc_cfg_bn(d.cfg);
+    const PackDesc& q = pd[i];
+    // A side: 128-row boxes; B side: bn-row boxes
+    const long long sa_hi = swap ? q.b_hi : q.a_hi, sa_lo = swap ? q.b_lo : q.a_lo;
+    const long long sb_hi = swap ? q.a_hi : q.b_hi, sb_lo = swap ? q.a_lo : q.b_lo;
+    const int ra = swap ? d.N : d.M, rb = swap ? d.M : d.N;
+    bool ok = encode_panel(&tm[4 * i + 0], t->kind, ws + sa_hi, d.K, ra, q.kpad, kTcBM) &&
+              encode_panel(&tm[4 * i + 1], t->kind, ws + sa_lo, d.K, ra, q.kpad, kTcBM) &&
+              encode_panel(&tm[4 * i + 2], t->kind, ws + sb_hi, d.K, rb, q.kpad, bn) &&
+              encode_panel(&tm[4 * i + 3], t->kind, ws + sb_lo, d.K, rb, q.kpad, bn);
+    if (!ok)
+      return set_error(BGEMM_ERROR_INTERNAL, 0, i, "tensor map encoding failed for matrix %d", i);
+  }
+  std::memcpy(h + off_pd, pd.data(), sizeof(PackDesc) * (size_t)batch);
+  if (!jobs.empty()) std::memcpy(h + off_jobs, jobs.data(), sizeof(PackJob) * jobs.size());
+  char* dm = static_cast<char*>(t->d_mem);
+  t->d_tmaps = reinterpret_cast<CUtensorMap*>(dm + off_tm);
+  t->d_pdescs = reinterpret_cast<PackDesc*>(dm + off_pd);
+  t->d_jobs = reinterpret_cast<PackJob*>(dm + off_jobs);
+  t->d_err = reinterpret_cast<int*>(dm + off_err);
+  e = cudaMemcpyAsync(t->d_mem, t->h_pin, total, cudaMemcpyHostToDevice, stream);
+  if (e != cudaSuccess) return cuda_error(e, "tensor-core descriptor upload");
+  p->info.workspace_bytes = t->ws_bytes;
+  p->info.device_bytes += t->ws_bytes + total;
+  p->info.kernels_per_execute = 2;
+  return BGEMM_SUCCESS;
+}
+
+bgemm_status_t tc_execute(bgemm_plan_s* p, float alpha, const float* const* dA,
+                          const float* const* dB, float beta, float* const* dC,
+                          cudaStream_t stream) {
+  TcPlan* t = p->tc;
+  TcPackParams pp{p->d_descs, t->d_pdescs, t->d_jobs, t->n_jobs, t->kind, t->split,
+                  static_cast<char*>(t->d_ws), dA, dB};
+  cudaError_t e = tc_pack_launch(pp, t->pack_grid, stream);
+  if (e != cudaSuccess) return cuda_error(e, "split/pack launch");
+  TcGemmParams gp{p->d_descs, p->d_items, p->n_items, p->d_counters, t->d_tmaps, alpha, beta,
+                  dC, t->d_err, 2000000000ull};
+  e = tc_gemm_launch(t->kind, t->split, gp, p->grid, stream);
+  if (e != cudaSuccess) return cuda_error(e, "tcgen05 GEMM launch");
+  return BGEMM_SUCCESS;
+}
+
+bgemm_status_t tc_check_device(bgemm_plan_s* p, cudaStream_t) {
+  TcPlan* t = p->tc;
+  int err = 0;
+  cudaError_t e = cudaMemcpy(&err, t->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_error(e, "device error word");
+  if (err) {
+    cudaMemset(t->d_err, 0, sizeof(int));
+    return set_error(BGEMM_ERROR_DEVICE_TIMEOUT, 0, -1,
+                     "a bounded wait in the tensor-core kernel expired; results are invalid");
+  }
+  return BGEMM_SUCCESS;
+}
+
+void tc_plan_release(bgemm_plan_s* p) {
+  TcPlan* t = p->tc;
+  if (!t) return;
+  if (t->d_ws) cudaFree(t->d_ws);
+  if (t->d_mem) cudaFree(t->d_mem);
+  if (t->h_pin) cudaFreeHost(t->h_pin);
+  delete t;
+  p->tc = nullptr;
+}
 
 }  // namespace bgemm

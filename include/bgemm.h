@@ -81,6 +81,8 @@ typedef struct bgemm_plan_info {
   double min_bytes;         /* compulsory HBM bytes: 4*(MK + KN + MN(1 + [beta!=0])) at beta=0 */
   size_t device_bytes;      /* descriptors + queue + workspace owned by the plan */
   size_t workspace_bytes;   /* split-operand workspace (tensor-core modes)   */
+  int kernels_per_execute;  /* kernel launches one bgemm_plan_execute makes  */
+  int reserved[7];
 } bgemm_plan_info_t;
 
 /* Options for bgemm_plan_create_ex (zero-initialise, then set fields). */
