@@ -12,14 +12,23 @@
 //   tc_gemm_kernel  one persistent CTA per SM pulls output tiles from the
 //                   largest-first queue.  Warp 0 (one lane) is the TMA
 //                   producer and tile scheduler, warp 1 (one lane) issues
-//                   tcgen05.mma into a double-buffered TMEM accumulator,
-//                   warps 2-5 drain TMEM (tcgen05.ld), apply alpha/beta and
-//                   store C.  Per 128-byte K slice a stage holds the hi (and
-//                   lo) tiles of both sides, TMA-loaded with 128-byte swizzle
-//                   through per-matrix tensor maps.
-// Split modes keep hi*hi in one TMEM accumulator and hi*lo + lo*hi in a
-// second, added in FP32 at the end, so the small terms are not rounded
-// against the large partial sums.
+//                   tcgen05.mma into TMEM, warps 2-5 drain TMEM (tcgen05.ld),
+//                   apply alpha/beta and store C.  Per 128-byte K slice a
+//                   stage holds the hi (and lo) tiles of both sides,
+//                   TMA-loaded with 128-byte swizzle through per-matrix
+//                   tensor maps.
+//
+// Accumulation.  The tensor core adds products into its FP32 accumulator
+// with truncation, so a long chain of MMAs into one accumulator drifts
+// toward zero (measured on GB300: -1.1e-7 of sum|ab| at K = 2048, against
+// 2e-8 unbiased for an FP32 fma chain).  The split modes therefore never let
+// a chain run long: every group of MMAs (32 k, or 8 k for matrices with
+// K <= 64) accumulates into a fresh buffer of a 4-deep TMEM ring -- the
+// small hi*lo and lo*hi products first, hi*hi last -- and the epilogue warps
+// add each finished group into FP32 registers with round-to-nearest while
+// the MMAs of the next groups run.  The single-product TF32 mode keeps one
+// accumulator per tile (double-buffered across tiles); its error is set by
+// the TF32 operand rounding anyway.
 //
 // Every wait on an mbarrier is bounded (global timer); on expiry the kernel
 // sets an error flag, lets in-flight copies and MMAs land, frees TMEM and
@@ -45,9 +54,16 @@ struct Geo {
   static constexpr int NP = SPLIT ? 2 : 1;
   static constexpr int STAGE = (kABytes + kBBytes) * NP;
   static constexpr int S = SPLIT ? 3 : 6;
-  static constexpr int NBAR = 2 * S + 2 * kSchedSlots + 4 + 1;
+  // TMEM accumulator buffers of 128 columns: a 4-deep group ring (split
+  // modes) or 2 tile buffers (single product)
+  static constexpr int NACC = SPLIT ? 4 : 2;
+  static constexpr int NBAR = 2 * S + 2 * kSchedSlots + 2 * NACC + 1;
   static constexpr int BYTES = S * STAGE + NBAR * 8 + kSchedSlots * 4 + 16 + 1024;
 };
+
+// Matrices with K at most this many elements promote every MMA (8 k for
+// TF32, 16 k for BF16) instead of every 128-byte slice.
+constexpr int kFineK = 64;
 
 // ------------------------------------------------------------- PTX glue --
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -228,8 +244,39 @@ __device__ __forceinline__ void put(char* hi, char* lo, long long idx, float x, 
   }
 }
 
+// Splits four consecutive k of one packed row and stores hi (and lo) with one
+// 16-byte (TF32) or 8-byte (BF16) store each; idx is a multiple of 4.
+__device__ __forceinline__ void put4(char* hi, char* lo, long long idx, const float* x, int kind,
+                                     int split) {
+  float h[4], l[4];
+  const int drop = (kind == kKindTF32) ? 13 : 16;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    h[i] = round_keep(x[i], drop);
+    const bool fin = (__float_as_uint(x[i]) & 0x7f800000u) != 0x7f800000u;
+    l[i] = fin ? round_keep(x[i] - h[i], drop) : 0.0f;
+  }
+  if (kind == kKindTF32) {
+    *reinterpret_cast<float4*>(reinterpret_cast<float*>(hi) + idx) = make_float4(h[0], h[1], h[2], h[3]);
+    if (split)
+      *reinterpret_cast<float4*>(reinterpret_cast<float*>(lo) + idx) = make_float4(l[0], l[1], l[2], l[3]);
+  } else {
+    auto pk = [](float a, float b) {
+      return (__float_as_uint(a) >> 16) | (__float_as_uint(b) & 0xFFFF0000u);
+    };
+    *reinterpret_cast<uint2*>(reinterpret_cast<uint16_t*>(hi) + idx) = make_uint2(pk(h[0], h[1]), pk(h[2], h[3]));
+    if (split)
+      *reinterpret_cast<uint2*>(reinterpret_cast<uint16_t*>(lo) + idx) = make_uint2(pk(l[0], l[1]), pk(l[2], l[3]));
+  }
+}
+
+// One job = 32 packed rows of one operand, walked in chunks of 64 k.  Each
+// thread issues all eight of its loads for a chunk before it stores, and
+// writes four consecutive k per store (rows are 16-byte aligned, so packed
+// writes are full vectors; the K tail and rows past M/N are masked).
 __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
-  __shared__ float t[32][33];
+  __shared__ float t[64][33];
+  const int tid = threadIdx.x;
   for (int j = blockIdx.x; j < p.n_jobs; j += gridDim.x) {
     const PackJob job = p.jobs[j];
     const MatDesc d = p.descs[job.mat];
@@ -237,34 +284,78 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
     const int K = d.K;
     const long long kpad = pd.kpad;
     if (job.op == 0) {
+      // A (column-major M x K) -> rows m of K: transpose through shared memory
       const float* A = p.A[job.mat];
       const long long lda = d.lda;
       char* hi = p.ws + pd.a_hi;
       char* lo = p.ws + pd.a_lo;
-      for (int k0 = 0; k0 < K; k0 += 32) {
-        for (int e = threadIdx.x; e < 1024; e += 256) {
-          const int kk = e >> 5, mm = e & 31;
-          const int m = job.r0 + mm, k = k0 + kk;
-          t[kk][mm] = (m < d.M && k < K) ? A[m + k * lda] : 0.0f;
+      const int mm = tid & 31;
+      const int m = job.r0 + mm;
+      for (int k0 = 0; k0 < K; k0 += 64) {
+        float v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int k = k0 + (tid >> 5) + 8 * i;
+          v[i] = (m < d.M && k < K) ? A[m + k * lda] : 0.0f;
         }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) t[(tid >> 5) + 8 * i][mm] = v[i];
         __syncthreads();
-        for (int e = threadIdx.x; e < 1024; e += 256) {
-          const int mm = e >> 5, kk = e & 31;
-          const int m = job.r0 + mm, k = k0 + kk;
-          if (m < d.M && k < K) put(hi, lo, m * kpad + k, t[kk][mm], p.kind, p.split);
+        const int wm = tid >> 3;           // packed row within the strip
+        const int wk = (tid & 7) * 4;      // first of four k
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const int kk = wk + 32 * h2;
+          const int k = k0 + kk;
+          const int mr = job.r0 + wm;
+          if (mr < d.M && k < K) {
+            float x[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) x[i] = t[kk + i][wm];
+            if (k + 4 <= K) {
+              put4(hi, lo, mr * kpad + k, x, p.kind, p.split);
+            } else {
+              for (int i = 0; i < 4 && k + i < K; ++i)
+                put(hi, lo, mr * kpad + k + i, x[i], p.kind, p.split);
+            }
+          }
         }
         __syncthreads();
       }
     } else {
+      // B (column-major K x N) is already rows n of K
       const float* B = p.B[job.mat];
       const long long ldb = d.ldb;
       char* hi = p.ws + pd.b_hi;
       char* lo = p.ws + pd.b_lo;
-      for (int k0 = 0; k0 < K; k0 += 32) {
-        for (int e = threadIdx.x; e < 1024; e += 256) {
-          const int nn = e >> 5, kk = e & 31;
-          const int n = job.r0 + nn, k = k0 + kk;
-          if (n < d.N && k < K) put(hi, lo, n * kpad + k, B[k + n * ldb], p.kind, p.split);
+      const int nn = tid >> 3;
+      const int n = job.r0 + nn;
+      const int wk = (tid & 7) * 4;
+      if (n >= d.N) continue;
+      const float* col = B + n * ldb;
+      const bool vec = ((reinterpret_cast<uintptr_t>(col) & 15u) == 0);
+      for (int k0 = 0; k0 < K; k0 += 64) {
+        float x[2][4];
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const int k = k0 + wk + 32 * h2;
+          if (vec && k + 4 <= K) {
+            const float4 f = *reinterpret_cast<const float4*>(col + k);
+            x[h2][0] = f.x; x[h2][1] = f.y; x[h2][2] = f.z; x[h2][3] = f.w;
+          } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) x[h2][i] = (k + i < K) ? col[k + i] : 0.0f;
+          }
+        }
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const int k = k0 + wk + 32 * h2;
+          if (k + 4 <= K) {
+            put4(hi, lo, n * kpad + k, x[h2], p.kind, p.split);
+          } else {
+            for (int i = 0; i < 4 && k + i < K; ++i)
+              put(hi, lo, n * kpad + k + i, x[h2][i], p.kind, p.split);
+          }
         }
       }
     }
@@ -290,9 +381,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
   auto empty = [&](int s) { return bar0 + 8u * (S + s); };
   auto sfull = [&](int s) { return bar0 + 8u * (2 * S + s); };
   auto sempty = [&](int s) { return bar0 + 8u * (2 * S + kSchedSlots + s); };
+  constexpr int NACC = G::NACC;
   auto tfull = [&](int s) { return bar0 + 8u * (2 * S + 2 * kSchedSlots + s); };
-  auto tempty = [&](int s) { return bar0 + 8u * (2 * S + 2 * kSchedSlots + 2 + s); };
-  const uint32_t drain = bar0 + 8u * (2 * S + 2 * kSchedSlots + 4);
+  auto tempty = [&](int s) { return bar0 + 8u * (2 * S + 2 * kSchedSlots + NACC + s); };
+  const uint32_t drain = bar0 + 8u * (2 * S + 2 * kSchedSlots + 2 * NACC);
   volatile int* slots = reinterpret_cast<volatile int*>(bars + G::NBAR);
   volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(slots + kSchedSlots);
   volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
@@ -309,7 +401,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
       mbar_init(sfull(s), 1);
       mbar_init(sempty(s), 1 + 4);
     }
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < NACC; ++s) {
       mbar_init(tfull(s), 1);
       mbar_init(tempty(s), 4);
     }
@@ -396,38 +488,83 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
         const int bn = tc_cfg_bn(d.cfg);
         const uint32_t idesc = make_idesc<KIND>(bn);
         const int nk = (d.K + KE - 1) / KE;
-        if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) break;
-        tc_fence_after();
-        const uint32_t d_main = tmem + acc.idx * 256u;
-        const uint32_t d_corr = d_main + 128u;
         bool ok = true;
-        for (int kb = 0; kb < nk; ++kb) {
-          if (!wait_bounded(full(st.idx), st.phase, p.error, abort, p.timeout_ns)) {
-            ok = false;
-            break;
-          }
-          tc_fence_after();
-          const uint32_t sa = sbase + st.idx * G::STAGE;
-          const uint32_t sb = sa + kABytes * G::NP;
-#pragma unroll
-          for (int s = 0; s < NSUB; ++s) {
-            const uint64_t ah = sw128_desc(sa + 32u * s);
-            const uint64_t bh = sw128_desc(sb + 32u * s);
-            const uint32_t accum = (kb > 0 || s > 0) ? 1u : 0u;
-            mma<KIND>(d_main, ah, bh, idesc, accum);
-            if (SPLIT) {
-              const uint64_t al = sw128_desc(sa + kABytes + 32u * s);
-              const uint64_t bl = sw128_desc(sb + kBBytes + 32u * s);
-              mma<KIND>(d_corr, ah, bl, idesc, accum);
-              mma<KIND>(d_corr, al, bh, idesc, 1u);
+        if constexpr (SPLIT) {
+          // group-promoted accumulation (see the file comment)
+          const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);  // MMAs of K per product
+          const bool fine = d.K <= kFineK;
+          for (int kb = 0; kb < nk && ok; ++kb) {
+            if (!wait_bounded(full(st.idx), st.phase, p.error, abort, p.timeout_ns)) {
+              ok = false;
+              break;
             }
+            tc_fence_after();
+            const uint32_t sa = sbase + st.idx * G::STAGE;
+            const uint32_t sb = sa + kABytes * G::NP;
+            const int s_end = min(NSUB, nsub - kb * NSUB);
+            if (fine) {
+              for (int s = 0; s < s_end; ++s) {
+                if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort,
+                                  p.timeout_ns)) {
+                  ok = false;
+                  break;
+                }
+                tc_fence_after();
+                const uint32_t buf = tmem + acc.idx * 128u;
+                const uint64_t ah = sw128_desc(sa + 32u * s), al = sw128_desc(sa + kABytes + 32u * s);
+                const uint64_t bh = sw128_desc(sb + 32u * s), bl = sw128_desc(sb + kBBytes + 32u * s);
+                mma<KIND>(buf, al, bh, idesc, 0u);
+                mma<KIND>(buf, ah, bl, idesc, 1u);
+                mma<KIND>(buf, ah, bh, idesc, 1u);
+                mma_commit(tfull(acc.idx));
+                acc.next(NACC);
+              }
+            } else {
+              if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
+                ok = false;
+                break;
+              }
+              tc_fence_after();
+              const uint32_t buf = tmem + acc.idx * 128u;
+              for (int s = 0; s < s_end; ++s) {
+                mma<KIND>(buf, sw128_desc(sa + kABytes + 32u * s), sw128_desc(sb + 32u * s), idesc,
+                          s > 0 ? 1u : 0u);
+                mma<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + kBBytes + 32u * s), idesc,
+                          1u);
+              }
+              for (int s = 0; s < s_end; ++s)
+                mma<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
+              mma_commit(tfull(acc.idx));
+              acc.next(NACC);
+            }
+            mma_commit(empty(st.idx));
+            st.next(S);
           }
-          mma_commit(empty(st.idx));
-          st.next(S);
+        } else {
+          if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) break;
+          tc_fence_after();
+          const uint32_t d_main = tmem + acc.idx * 256u;
+          for (int kb = 0; kb < nk; ++kb) {
+            if (!wait_bounded(full(st.idx), st.phase, p.error, abort, p.timeout_ns)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sa = sbase + st.idx * G::STAGE;
+            const uint32_t sb = sa + kABytes * G::NP;
+#pragma unroll
+            for (int s = 0; s < NSUB; ++s)
+              mma<KIND>(d_main, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc,
+                        (kb > 0 || s > 0) ? 1u : 0u);
+            mma_commit(empty(st.idx));
+            st.next(S);
+          }
+          if (ok) {
+            mma_commit(tfull(acc.idx));
+            acc.next(NACC);
+          }
         }
         if (!ok) break;
-        mma_commit(tfull(acc.idx));
-        acc.next(2);
       }
       // all MMAs issued by this thread complete before TMEM is freed
       mma_commit(drain);
@@ -454,36 +591,82 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
       float* C = p.C[ti.mat];
       const int bn = tc_cfg_bn(d.cfg);
       const bool swap = tc_cfg_swap(d.cfg);
-      if (lane == 0) ok = wait_bounded(tfull(acc.idx), acc.phase, p.error, abort, p.timeout_ns);
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-      if (!ok) break;
-      tc_fence_after();
       const int row = ti.tm * kTcBM + q * 32 + lane;  // A-side row
       const long long ldc = d.ldc;
-      const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + acc.idx * 256u;
-      const bool kzero = d.K == 0;
-      for (int c0 = 0; c0 < bn; c0 += 16) {
-        float v[16], u[16];
-        tmem_ld16(tb + c0, v);
-        if (SPLIT) tmem_ld16(tb + 128u + c0, u);
-        tmem_wait_ld();
-        const int col0 = ti.tn * bn + c0;  // B-side index of v[0]
+      const int col_base = ti.tn * bn;                // B-side index of column 0
+      if constexpr (SPLIT) {
+        // promote every MMA group into FP32 registers (round to nearest)
+        const int nk = (d.K + KE - 1) / KE;
+        const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
+        const int ngroups = (d.K <= kFineK) ? nsub : nk;
+        float r[kTcMaxBN];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          float x = SPLIT ? v[j] + u[j] : v[j];
-          if (kzero) x = 0.0f;
-          const int m = swap ? col0 + j : row;
-          const int n = swap ? row : col0 + j;
-          if (m < d.M && n < d.N) {
-            float* c = C + m + n * ldc;
-            *c = (beta == 0.0f) ? alpha * x : fmaf(alpha, x, beta * *c);
+        for (int j = 0; j < kTcMaxBN; ++j) r[j] = 0.0f;
+        for (int g = 0; g < ngroups; ++g) {
+          if (lane == 0) ok = wait_bounded(tfull(acc.idx), acc.phase, p.error, abort, p.timeout_ns);
+          ok = __shfl_sync(0xffffffffu, ok, 0);
+          if (!ok) break;
+          tc_fence_after();
+          const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + acc.idx * 128u;
+#pragma unroll
+          for (int c = 0; c < kTcMaxBN / 16; c += 2) {
+            if (c * 16 < bn) {
+              float v0[16], v1[16];
+              tmem_ld16(tb + c * 16, v0);
+              if ((c + 1) * 16 < bn) tmem_ld16(tb + (c + 1) * 16, v1);
+              tmem_wait_ld();
+#pragma unroll
+              for (int j = 0; j < 16; ++j) r[c * 16 + j] += v0[j];
+              if ((c + 1) * 16 < bn) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) r[(c + 1) * 16 + j] += v1[j];
+              }
+            }
+          }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(tempty(acc.idx));
+          acc.next(NACC);
+        }
+        if (!ok) break;
+#pragma unroll
+        for (int j = 0; j < kTcMaxBN; ++j) {
+          if (j < bn) {
+            const int m = swap ? col_base + j : row;
+            const int n = swap ? row : col_base + j;
+            if (m < d.M && n < d.N) {
+              float* c = C + m + n * ldc;
+              *c = (beta == 0.0f) ? alpha * r[j] : fmaf(alpha, r[j], beta * *c);
+            }
           }
         }
+      } else {
+        if (lane == 0) ok = wait_bounded(tfull(acc.idx), acc.phase, p.error, abort, p.timeout_ns);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) break;
+        tc_fence_after();
+        const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + acc.idx * 256u;
+        const bool kzero = d.K == 0;
+        for (int c0 = 0; c0 < bn; c0 += 16) {
+          float v[16];
+          tmem_ld16(tb + c0, v);
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const float x = kzero ? 0.0f : v[j];
+            const int m = swap ? col_base + c0 + j : row;
+            const int n = swap ? row : col_base + c0 + j;
+            if (m < d.M && n < d.N) {
+              float* c = C + m + n * ldc;
+              *c = (beta == 0.0f) ? alpha * x : fmaf(alpha, x, beta * *c);
+            }
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(tempty(acc.idx));
+        acc.next(NACC);
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(tempty(acc.idx));
-      acc.next(2);
     }
   }
 
