@@ -47,7 +47,7 @@ namespace {
 constexpr int kABytes = kTcBM * 128;        // 128 rows x 128 bytes of K
 constexpr int kBBytes = kTcMaxBN * 128;     // up to 128 rows x 128 bytes
 constexpr int kSchedSlots = 4;
-constexpr int kThreads = 192;
+constexpr int kThreads = 64 + 8 * 32;  // producer, MMA, 8 epilogue warps
 
 template <int SPLIT>
 struct Geo {
@@ -62,8 +62,13 @@ struct Geo {
 };
 
 // Matrices with K at most this many elements promote every MMA (8 k for
-// TF32, 16 k for BF16) instead of every 128-byte slice.
+// TF32, 16 k for BF16); larger K promotes every kGroupKB 128-byte slices.
 constexpr int kFineK = 64;
+constexpr int kGroupKB = 2;
+// Epilogue: 8 warps, two per TMEM lane quadrant, each owning half of the
+// 128 accumulator columns.
+constexpr int kEpiWarps = 8;
+constexpr int kEpiCols = kTcMaxBN / 2;
 
 // ------------------------------------------------------------- PTX glue --
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -399,11 +404,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
     }
     for (int s = 0; s < kSchedSlots; ++s) {
       mbar_init(sfull(s), 1);
-      mbar_init(sempty(s), 1 + 4);
+      mbar_init(sempty(s), 1 + kEpiWarps);
     }
     for (int s = 0; s < NACC; ++s) {
       mbar_init(tfull(s), 1);
-      mbar_init(tempty(s), 4);
+      mbar_init(tempty(s), kEpiWarps);
     }
     mbar_init(drain, 1);
     *abort = 0;
@@ -520,22 +525,29 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
                 acc.next(NACC);
               }
             } else {
-              if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
-                ok = false;
-                break;
+              // a group spans kGroupKB slices; small products of each slice first
+              const bool first = (kb % kGroupKB) == 0;
+              if (first) {
+                if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort,
+                                  p.timeout_ns)) {
+                  ok = false;
+                  break;
+                }
+                tc_fence_after();
               }
-              tc_fence_after();
               const uint32_t buf = tmem + acc.idx * 128u;
               for (int s = 0; s < s_end; ++s) {
                 mma<KIND>(buf, sw128_desc(sa + kABytes + 32u * s), sw128_desc(sb + 32u * s), idesc,
-                          s > 0 ? 1u : 0u);
+                          (first && s == 0) ? 0u : 1u);
                 mma<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + kBBytes + 32u * s), idesc,
                           1u);
               }
               for (int s = 0; s < s_end; ++s)
                 mma<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
-              mma_commit(tfull(acc.idx));
-              acc.next(NACC);
+              if ((kb % kGroupKB) == kGroupKB - 1 || kb == nk - 1) {
+                mma_commit(tfull(acc.idx));
+                acc.next(NACC);
+              }
             }
             mma_commit(empty(st.idx));
             st.next(S);
@@ -573,7 +585,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
     __syncwarp();
   } else {
     // ------------------------------------------------------------ epilogue
-    const int q = warp & 3;  // this warp may read TMEM lanes 32q .. 32q+31
+    const int q = warp & 3;             // this warp may read TMEM lanes 32q .. 32q+31
+    const int half = (warp - 2) >> 2;   // and owns accumulator columns half*64 ..
     Ring sc, acc;
     const float alpha = p.alpha, beta = p.beta;
     for (;;) {
@@ -593,79 +606,69 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
       const bool swap = tc_cfg_swap(d.cfg);
       const int row = ti.tm * kTcBM + q * 32 + lane;  // A-side row
       const long long ldc = d.ldc;
-      const int col_base = ti.tn * bn;                // B-side index of column 0
+      const int c_lo = half * kEpiCols;               // first accumulator column owned
+      const int ncols = max(0, min(kEpiCols, bn - c_lo));
+      const int col_base = ti.tn * bn + c_lo;         // B-side index of owned column 0
+      float r[kEpiCols];
+#pragma unroll
+      for (int j = 0; j < kEpiCols; ++j) r[j] = 0.0f;
       if constexpr (SPLIT) {
         // promote every MMA group into FP32 registers (round to nearest)
         const int nk = (d.K + KE - 1) / KE;
         const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
-        const int ngroups = (d.K <= kFineK) ? nsub : nk;
-        float r[kTcMaxBN];
-#pragma unroll
-        for (int j = 0; j < kTcMaxBN; ++j) r[j] = 0.0f;
+        const int ngroups = (d.K <= kFineK) ? nsub : (nk + kGroupKB - 1) / kGroupKB;
         for (int g = 0; g < ngroups; ++g) {
           if (lane == 0) ok = wait_bounded(tfull(acc.idx), acc.phase, p.error, abort, p.timeout_ns);
           ok = __shfl_sync(0xffffffffu, ok, 0);
           if (!ok) break;
           tc_fence_after();
-          const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + acc.idx * 128u;
+          const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + acc.idx * 128u + c_lo;
+          float v[kEpiCols];
 #pragma unroll
-          for (int c = 0; c < kTcMaxBN / 16; c += 2) {
-            if (c * 16 < bn) {
-              float v0[16], v1[16];
-              tmem_ld16(tb + c * 16, v0);
-              if ((c + 1) * 16 < bn) tmem_ld16(tb + (c + 1) * 16, v1);
-              tmem_wait_ld();
+          for (int c = 0; c < kEpiCols / 16; ++c)
+            if (c * 16 < ncols) tmem_ld16(tb + c * 16, v + c * 16);
+          tmem_wait_ld();
 #pragma unroll
-              for (int j = 0; j < 16; ++j) r[c * 16 + j] += v0[j];
-              if ((c + 1) * 16 < bn) {
+          for (int c = 0; c < kEpiCols / 16; ++c)
+            if (c * 16 < ncols) {
 #pragma unroll
-                for (int j = 0; j < 16; ++j) r[(c + 1) * 16 + j] += v1[j];
-              }
+              for (int j = 0; j < 16; ++j) r[c * 16 + j] += v[c * 16 + j];
             }
-          }
           tc_fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(tempty(acc.idx));
           acc.next(NACC);
         }
         if (!ok) break;
-#pragma unroll
-        for (int j = 0; j < kTcMaxBN; ++j) {
-          if (j < bn) {
-            const int m = swap ? col_base + j : row;
-            const int n = swap ? row : col_base + j;
-            if (m < d.M && n < d.N) {
-              float* c = C + m + n * ldc;
-              *c = (beta == 0.0f) ? alpha * r[j] : fmaf(alpha, r[j], beta * *c);
-            }
-          }
-        }
       } else {
         if (lane == 0) ok = wait_bounded(tfull(acc.idx), acc.phase, p.error, abort, p.timeout_ns);
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (!ok) break;
         tc_fence_after();
-        const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + acc.idx * 256u;
-        const bool kzero = d.K == 0;
-        for (int c0 = 0; c0 < bn; c0 += 16) {
-          float v[16];
-          tmem_ld16(tb + c0, v);
-          tmem_wait_ld();
+        const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + acc.idx * 256u + c_lo;
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const float x = kzero ? 0.0f : v[j];
-            const int m = swap ? col_base + c0 + j : row;
-            const int n = swap ? row : col_base + c0 + j;
-            if (m < d.M && n < d.N) {
-              float* c = C + m + n * ldc;
-              *c = (beta == 0.0f) ? alpha * x : fmaf(alpha, x, beta * *c);
-            }
-          }
+        for (int c = 0; c < kEpiCols / 16; ++c)
+          if (c * 16 < ncols) tmem_ld16(tb + c * 16, r + c * 16);
+        tmem_wait_ld();
+        if (d.K == 0) {
+#pragma unroll
+          for (int j = 0; j < kEpiCols; ++j) r[j] = 0.0f;
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(tempty(acc.idx));
         acc.next(NACC);
+      }
+#pragma unroll
+      for (int j = 0; j < kEpiCols; ++j) {
+        if (j < ncols) {
+          const int m = swap ? col_base + j : row;
+          const int n = swap ? row : col_base + j;
+          if (m < d.M && n < d.N) {
+            float* c = C + m + n * ldc;
+            *c = (beta == 0.0f) ? alpha * r[j] : fmaf(alpha, r[j], beta * *c);
+          }
+        }
       }
     }
   }
