@@ -26,7 +26,8 @@ struct TcPlan;
 // MatDesc::aux bit of the tensor-core modes: the matrix runs with A and B
 // swapped (C^T = B^T A^T), so the MMA's M dimension walks N.
 constexpr int kTcSwapFlag = 1 << 30;
-constexpr int kTcNumCfgs = 8;
+// ids 0..7: one-SM tiles; ids 8..15: CTA-pair tiles (split modes)
+constexpr int kTcNumCfgs = 16;
 
 }  // namespace bgemm
 

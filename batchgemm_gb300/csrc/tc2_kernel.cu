@@ -1,0 +1,355 @@
+// tc2_kernel.cu -- the split-precision tensor-core GEMM on CTA pairs
+// (tcgen05 cta_group::2, two SMs per output tile).
+//
+// Each cluster of two CTAs owns a 256 x BN output tile (BN = 64, 128 or 256)
+// of one matrix: CTA r loads rows [128r, 128r + 128) of the A side and rows
+// [r*BN/2, (r+1)*BN/2) of the B side (hi and lo halves) with TMA into its own
+// shared memory, the leader CTA issues every cta_group::2 MMA, and each CTA
+// receives its 128 x BN slice of the accumulator in its own TMEM.  Per
+// 128-byte K slice a CTA loads at most 64 KB for 128 x 256 outputs -- half
+// the L2 traffic per flop of the one-SM kernel (tc_kernel.cu), which is what
+// bounds that kernel.
+//
+// Accumulation is group-promoted exactly as in tc_kernel.cu: each group (one
+// 128-byte K slice, or one MMA for K <= 64) accumulates into a fresh 256-column
+// TMEM buffer (2-deep ring) with the small products first, and the epilogue
+// warps of both CTAs add it into FP32 registers with round-to-nearest.
+//
+// Scheduling is static and needs no traffic between the CTAs: cluster c
+// takes queue items c, 2C-1-c, 2C+c, ... (a snake over the largest-first
+// queue, C clusters), so both CTAs of a pair walk the same tiles.
+//
+// Synchronisation across the pair:
+//   full[s]   leader only: its producer expects the bytes of both CTAs; the
+//             peer's TMA completes on the leader's barrier (cta_group::2 TMA);
+//   empty[s]  both CTAs: the leader's commit is multicast to the pair;
+//   tfull[b]  both CTAs: multicast commit when a group's MMAs finish;
+//   tempty[b] leader only: 16 arrivals (8 epilogue warps x 2 CTAs).
+// All waits are bounded as in tc_kernel.cu.
+#include <stdint.h>
+
+#include "tc_ptx.h"
+
+namespace bgemm {
+namespace {
+
+constexpr int kRows = 128;                 // A-side rows per CTA
+constexpr int kA = kRows * 128;            // 16 KB per part
+constexpr int kB = 128 * 128;              // B-side half: up to 128 rows
+constexpr int kStage = 2 * (kA + kB);      // hi + lo of both sides: 64 KB
+constexpr int kS = 3;
+constexpr int kNAcc = 2;                   // 256-column group buffers
+constexpr int kNBar = 2 * kS + 2 * kNAcc + 1;
+constexpr int kSmem = kS * kStage + kNBar * 8 + 16 + 1024;
+constexpr int kEpiWarps2 = 8;              // 2 per TMEM lane quadrant
+constexpr int kCols = 128;                 // accumulator columns per epilogue warp
+constexpr int kThreads2 = 64 + kEpiWarps2 * 32;
+constexpr int kFineK2 = 64;
+
+__device__ __forceinline__ int snake(int c, int t, int ncl) {
+  const int base = t * ncl;
+  return (t & 1) ? base + (ncl - 1 - c) : base + c;
+}
+
+template <int KIND>
+__device__ __forceinline__ uint32_t make_idesc_pair(int n) {
+  constexpr uint32_t fmt = (KIND == kKindTF32) ? 2u : 1u;
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(256 >> 4) << 24);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmParams p) {
+  constexpr int KE = (KIND == kKindTF32) ? 32 : 64;  // elements per 128-byte slice
+  constexpr int NSUB = 4;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
+  uint8_t* smem = smem_raw + pad;
+  const uint32_t sbase = raw + pad;
+  const uint32_t bar0 = sbase + kS * kStage;
+  auto full = [&](int s) { return bar0 + 8u * s; };
+  auto empty = [&](int s) { return bar0 + 8u * (kS + s); };
+  auto tfull = [&](int s) { return bar0 + 8u * (2 * kS + s); };
+  auto tempty = [&](int s) { return bar0 + 8u * (2 * kS + kNAcc + s); };
+  const uint32_t drain = bar0 + 8u * (2 * kS + 2 * kNAcc);
+  volatile uint32_t* tmem_slot =
+      reinterpret_cast<volatile uint32_t*>(smem + kS * kStage + kNBar * 8);
+  volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const uint32_t rank = cluster_ctarank();
+  const bool leader = rank == 0;
+  const int cl = blockIdx.x >> 1;
+  const int ncl = gridDim.x >> 1;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kS; ++s) {
+      mbar_init(full(s), 1);
+      mbar_init(empty(s), 1);
+    }
+    for (int s = 0; s < kNAcc; ++s) {
+      mbar_init(tfull(s), 1);
+      mbar_init(tempty(s), 2 * kEpiWarps2);
+    }
+    mbar_init(drain, 1);
+    *abort = 0;
+    fence_mbar_init();
+  }
+  cluster_sync();
+  if (warp == 1) {
+    tmem_alloc_pair(smem_u32(const_cast<uint32_t*>(tmem_slot)), 512);
+    tmem_relinquish_pair();
+  }
+  tc_fence_before();
+  __syncthreads();
+  cluster_sync();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      Ring st;
+      int inflight_phase[kS];
+      bool inflight[kS];
+      for (int s = 0; s < kS; ++s) inflight[s] = false, inflight_phase[s] = 0;
+      bool ok = true;
+      for (int t = 0; ok; ++t) {
+        const int it = snake(cl, t, ncl);
+        if (it >= p.n_items) break;
+        const TileItem ti = p.items[it];
+        const MatDesc d = p.descs[ti.mat];
+        const int bn = tc2_cfg_bn(d.cfg);
+        const int hb = bn >> 1;
+        const CUtensorMap* tm = p.tmaps + 4 * ti.mat;
+        const int nk = (d.K + KE - 1) / KE;
+        const uint32_t tx = 2u * 2u * (uint32_t)(kA + hb * 128);  // both CTAs, hi + lo
+        const int row_a = ti.tm * 256 + (int)rank * kRows;
+        const int row_b = ti.tn * bn + (int)rank * hb;
+        for (int kb = 0; kb < nk; ++kb) {
+          if (!wait_bounded(empty(st.idx), st.phase ^ 1u, p.error, abort, p.timeout_ns)) {
+            ok = false;
+            break;
+          }
+          const uint32_t sa = sbase + st.idx * kStage;
+          const uint32_t sb = sa + 2 * kA;
+          const uint32_t fb = mapa_shared(full(st.idx), 0);
+          if (leader) {
+            mbar_arrive_expect_tx(full(st.idx), tx);
+            inflight[st.idx] = true;
+            inflight_phase[st.idx] = st.phase;
+          }
+          tma_load_2d_pair(sa, tm + 0, kb * KE, row_a, fb);
+          tma_load_2d_pair(sa + kA, tm + 1, kb * KE, row_a, fb);
+          tma_load_2d_pair(sb, tm + 2, kb * KE, row_b, fb);
+          tma_load_2d_pair(sb + kB, tm + 3, kb * KE, row_b, fb);
+          st.next(kS);
+        }
+      }
+      // The leader's full barriers count the bytes of both CTAs: once every
+      // phase it expected has completed, no copy of either CTA is in flight.
+      if (leader) {
+        for (int s = 0; s < kS; ++s)
+          if (inflight[s])
+            wait_bounded(full(s), (uint32_t)inflight_phase[s], p.error, nullptr, p.timeout_ns);
+      }
+      if (!ok) {
+        const uint64_t t0 = gtimer();  // aborted: give stray copies time to land
+        while (gtimer() - t0 < 200000ull) {
+        }
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // -------------------------------------------------- MMA issue (leader)
+    if (lane == 0 && leader) {
+      Ring st, acc;
+      bool ok = true;
+      for (int t = 0; ok; ++t) {
+        const int it = snake(cl, t, ncl);
+        if (it >= p.n_items) break;
+        const TileItem ti = p.items[it];
+        const MatDesc d = p.descs[ti.mat];
+        const int bn = tc2_cfg_bn(d.cfg);
+        const uint32_t idesc = make_idesc_pair<KIND>(bn);
+        const int nk = (d.K + KE - 1) / KE;
+        const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
+        const bool fine = d.K <= kFineK2;
+        for (int kb = 0; kb < nk; ++kb) {
+          if (!wait_bounded(full(st.idx), st.phase, p.error, abort, p.timeout_ns)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = sbase + st.idx * kStage;
+          const uint32_t sb = sa + 2 * kA;
+          const int s_end = min(NSUB, nsub - kb * NSUB);
+          if (fine) {
+            for (int s = 0; s < s_end && ok; ++s) {
+              if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
+                ok = false;
+                break;
+              }
+              tc_fence_after();
+              const uint32_t buf = tmem + acc.idx * 256u;
+              mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + 32u * s), idesc, 0u);
+              mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + kB + 32u * s), idesc, 1u);
+              mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
+              mma_commit_pair(tfull(acc.idx));
+              acc.next(kNAcc);
+            }
+            if (!ok) break;
+          } else {
+            if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t buf = tmem + acc.idx * 256u;
+            for (int s = 0; s < s_end; ++s) {
+              mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + 32u * s), idesc,
+                             s > 0 ? 1u : 0u);
+              mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + kB + 32u * s), idesc,
+                             1u);
+            }
+            for (int s = 0; s < s_end; ++s)
+              mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
+            mma_commit_pair(tfull(acc.idx));
+            acc.next(kNAcc);
+          }
+          mma_commit_pair(empty(st.idx));
+          st.next(kS);
+        }
+      }
+      mma_commit_pair(drain);
+      wait_bounded(drain, 0, p.error, nullptr, p.timeout_ns);
+    }
+    __syncwarp();
+  } else {
+    // -------------------------------------------- epilogue (both CTAs)
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    Ring acc;
+    const float alpha = p.alpha, beta = p.beta;
+    for (int t = 0;; ++t) {
+      const int it = snake(cl, t, ncl);
+      if (it >= p.n_items) break;
+      const TileItem ti = p.items[it];
+      const MatDesc d = p.descs[ti.mat];
+      float* C = p.C[ti.mat];
+      const int bn = tc2_cfg_bn(d.cfg);
+      const bool swap = tc_cfg_swap(d.cfg);
+      const int row = ti.tm * 256 + (int)rank * kRows + q * 32 + lane;  // A-side row
+      const long long ldc = d.ldc;
+      const int c_lo = half * kCols;
+      const int ncols = max(0, min(kCols, bn - c_lo));
+      const int col_base = ti.tn * bn + c_lo;
+      const int nk = (d.K + KE - 1) / KE;
+      const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
+      const int ngroups = (d.K <= kFineK2) ? nsub : nk;
+      float r[kCols];
+#pragma unroll
+      for (int j = 0; j < kCols; ++j) r[j] = 0.0f;
+      int ok = 1;
+      for (int g = 0; g < ngroups; ++g) {
+        if (lane == 0) ok = wait_bounded(tfull(acc.idx), acc.phase, p.error, abort, p.timeout_ns);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) break;
+        tc_fence_after();
+        const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + acc.idx * 256u + c_lo;
+#pragma unroll
+        for (int c = 0; c < kCols / 16; c += 2) {
+          if (c * 16 < ncols) {
+            float v0[16], v1[16];
+            tmem_ld16(tb + c * 16, v0);
+            tmem_ld16(tb + (c + 1) * 16, v1);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              r[c * 16 + j] += v0[j];
+              r[(c + 1) * 16 + j] += v1[j];
+            }
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive_cluster(mapa_shared(tempty(acc.idx), 0));
+        acc.next(kNAcc);
+      }
+      if (!ok) break;
+#pragma unroll
+      for (int j = 0; j < kCols; ++j) {
+        if (j < ncols) {
+          const int m = swap ? col_base + j : row;
+          const int n = swap ? row : col_base + j;
+          if (m < d.M && n < d.N) {
+            float* c = C + m + n * ldc;
+            *c = (beta == 0.0f) ? alpha * r[j] : fmaf(alpha, r[j], beta * *c);
+          }
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  cluster_sync();
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc_pair(tmem, 512);
+}
+
+template <int KIND>
+cudaError_t launch2(const TcGemmParams& p, int grid, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tc2_gemm_kernel<KIND>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid, 1, 1);
+  cfg.blockDim = dim3(kThreads2, 1, 1);
+  cfg.dynamicSmemBytes = kSmem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, tc2_gemm_kernel<KIND>, p);
+}
+
+}  // namespace
+
+cudaError_t tc2_gemm_launch(int kind, const TcGemmParams& p, int grid, cudaStream_t s) {
+  if (grid < 2 || (grid & 1)) return cudaErrorInvalidValue;
+  if (kind == kKindTF32) return launch2<kKindTF32>(p, grid, s);
+  return launch2<kKindBF16>(p, grid, s);
+}
+
+int tc2_max_clusters() {
+  int n = 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2, 1, 1);
+  cfg.blockDim = dim3(kThreads2, 1, 1);
+  cfg.dynamicSmemBytes = kSmem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaFuncSetAttribute(tc2_gemm_kernel<kKindTF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       kSmem);
+  if (cudaOccupancyMaxActiveClusters(&n, tc2_gemm_kernel<kKindTF32>, &cfg) != cudaSuccess)
+    return 0;
+  return n;
+}
+
+}  // namespace bgemm

@@ -21,6 +21,12 @@ constexpr int kTcBM = 128;
 constexpr int kTcMaxBN = 128;
 __host__ __device__ constexpr int tc_cfg_bn(int cfg) { return 16 << (cfg & 3); }
 __host__ __device__ constexpr bool tc_cfg_swap(int cfg) { return (cfg & 4) != 0; }
+// CTA-pair configurations (ids 8..15): a 256 x BN tile on two SMs,
+// BN = 64, 128, 256 (ids with (cfg & 3) == 3 are unused); bit 2 swaps.
+constexpr int kTcPairCfg0 = 8;
+__host__ __device__ constexpr bool tc_cfg_pair(int cfg) { return cfg >= kTcPairCfg0; }
+__host__ __device__ constexpr int tc2_cfg_bn(int cfg) { return 64 << (cfg & 3); }
+__host__ __device__ constexpr bool tc2_cfg_valid(int cfg) { return (cfg & 3) != 3; }
 
 // One pre-pass job: split/pack a strip of 32 rows of one operand.
 struct PackJob {
@@ -64,5 +70,8 @@ struct TcGemmParams {
 cudaError_t tc_pack_launch(const TcPackParams& p, int grid, cudaStream_t s);
 cudaError_t tc_gemm_launch(int kind, int split, const TcGemmParams& p, int grid, cudaStream_t s);
 int tc_smem_bytes(int kind, int split);
+// CTA-pair kernel (split modes); grid = 2 x clusters
+cudaError_t tc2_gemm_launch(int kind, const TcGemmParams& p, int grid, cudaStream_t s);
+int tc2_max_clusters();
 
 }  // namespace bgemm

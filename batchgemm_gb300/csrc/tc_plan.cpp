@@ -27,6 +27,8 @@ struct TcPlan {
   int* d_err = nullptr;
   int n_jobs = 0;
   int pack_grid = 1;
+  bool pair = false;   // CTA-pair kernel (tc2_kernel.cu)
+  int clusters = 0;    // CTA pairs resident at once
 };
 
 static inline long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
@@ -35,18 +37,36 @@ static inline long long cdiv(long long a, long long b) { return (a + b - 1) / b;
 static double g_rate_ns = 7782.0;
 static int g_nprod = 3;
 static int g_kind = kKindTF32;
+static bool g_pair = false;
 
 // Modelled tile time: a fixed part plus the MMA time of K, where MMAs
-// narrower than 64 columns cost as much as 64 (operand reads dominate).
+// narrower than 64 columns cost as much as 64 (operand reads dominate).  A
+// CTA-pair tile runs on two SMs at once.  Only the configurations of the
+// plan's kernel (one-SM or CTA-pair) are offered.
 static bool tc_eval(int c, int M, int N, int K, long long* tiles, double* t_tile) {
+  if (tc_cfg_pair(c) != g_pair) return false;
+  if (g_pair && !tc2_cfg_valid(c)) return false;
   const bool swap = tc_cfg_swap(c);
-  const int bn = tc_cfg_bn(c);
+  const int bm = g_pair ? 256 : kTcBM;
+  const int bn = g_pair ? tc2_cfg_bn(c) : tc_cfg_bn(c);
   const long long ra = swap ? N : M, rb = swap ? M : N;
-  if (cdiv(ra, kTcBM) > 65535 || cdiv(rb, bn) > 65535) return false;
-  *tiles = cdiv(ra, kTcBM) * cdiv(rb, bn);
-  const double rate = g_rate_ns * (g_kind == kKindBF16 ? 2.0 : 1.0);
-  *t_tile = 1200.0 + 2.0 * kTcBM * std::max(bn, 64) * g_nprod * (double)K / rate;
+  if (cdiv(ra, bm) > 65535 || cdiv(rb, bn) > 65535) return false;
+  *tiles = cdiv(ra, bm) * cdiv(rb, bn);
+  const double rate = g_rate_ns * (g_kind == kKindBF16 ? 2.0 : 1.0) * (g_pair ? 2.0 : 1.0);
+  *t_tile = 1200.0 + 2.0 * bm * std::max(bn, 64) * g_nprod * (double)K / rate;
   return true;
+}
+
+// CTA pairs pay off when most of the work sits in matrices large enough to
+// fill 256-row tiles.
+static bool want_pairs(const int* M, const int* N, const int* K, int batch) {
+  double big = 0, all = 0;
+  for (int i = 0; i < batch; ++i) {
+    const double f = (double)M[i] * N[i] * K[i];
+    all += f;
+    if (std::max(M[i], N[i]) >= 256 && std::min(M[i], N[i]) >= 64) big += f;
+  }
+  return all > 0 && big >= 0.5 * all;
 }
 
 bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int* K, int batch,
@@ -56,17 +76,34 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
   t->split = (p->mode == BGEMM_MODE_TF32) ? 0 : 1;
   t->nprod = t->split ? 3 : 1;
   p->tc = t;
+  if (opt && opt->force_tile_config >= 0)
+    t->pair = tc_cfg_pair(opt->force_tile_config);
+  else
+    t->pair = t->split && want_pairs(M, N, K, batch);
+  if (t->pair && !t->split)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1,
+                     "CTA-pair tiles serve the split modes only");
+  if (t->pair) {
+    t->clusters = tc2_max_clusters();
+    if (t->clusters < 1) {
+      if (opt && opt->force_tile_config >= 0)
+        return set_error(BGEMM_ERROR_NOT_SUPPORTED, 11, -1, "no CTA pair fits on this device");
+      t->pair = false;
+    }
+  }
   static std::mutex mu;
   std::lock_guard<std::mutex> lk(mu);
   g_nprod = t->nprod;
   g_kind = t->kind;
-  const int slots = p->facts.num_sms * p->facts.tc_ctas_per_sm;
+  g_pair = t->pair;
+  const int slots = t->pair ? t->clusters : p->facts.num_sms * p->facts.tc_ctas_per_sm;
   return choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, slots, opt, mp);
 }
 
-void tc_tile_dims(bgemm_plan_s*, int, int, int, int cfg, int* bm, int* bn, MatDesc* d) {
-  *bm = kTcBM;
-  *bn = tc_cfg_bn(cfg);
+void tc_tile_dims(bgemm_plan_s* p, int, int, int, int cfg, int* bm, int* bn, MatDesc* d) {
+  const bool pair = p->tc->pair;
+  *bm = pair ? 256 : kTcBM;
+  *bn = pair ? tc2_cfg_bn(cfg) : tc_cfg_bn(cfg);
   d->aux = tc_cfg_swap(cfg) ? kTcSwapFlag : 0;
 }
 
@@ -172,16 +209,17 @@ bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream) {
     const MatDesc& d = hd[i];
     if (d.M == 0 || d.N == 0 || d.K == 0) continue;
     const bool swap = tc_cfg_swap(d.cfg);
-    const int bn = tc_cfg_bn(d.cfg);
+    // one SM: A-side boxes of 128 rows, B-side boxes of bn rows; a CTA pair
+    // loads per CTA 128 A-side rows and half of the bn B-side rows
+    const int bbox = t->pair ? tc2_cfg_bn(d.cfg) / 2 : tc_cfg_bn(d.cfg);
     const PackDesc& q = pd[i];
-    // A side: 128-row boxes; B side: bn-row boxes
     const long long sa_hi = swap ? q.b_hi : q.a_hi, sa_lo = swap ? q.b_lo : q.a_lo;
     const long long sb_hi = swap ? q.a_hi : q.b_hi, sb_lo = swap ? q.a_lo : q.b_lo;
     const int ra = swap ? d.N : d.M, rb = swap ? d.M : d.N;
     bool ok = encode_panel(&tm[4 * i + 0], t->kind, ws + sa_hi, d.K, ra, q.kpad, kTcBM) &&
               encode_panel(&tm[4 * i + 1], t->kind, ws + sa_lo, d.K, ra, q.kpad, kTcBM) &&
-              encode_panel(&tm[4 * i + 2], t->kind, ws + sb_hi, d.K, rb, q.kpad, bn) &&
-              encode_panel(&tm[4 * i + 3], t->kind, ws + sb_lo, d.K, rb, q.kpad, bn);
+              encode_panel(&tm[4 * i + 2], t->kind, ws + sb_hi, d.K, rb, q.kpad, bbox) &&
+              encode_panel(&tm[4 * i + 3], t->kind, ws + sb_lo, d.K, rb, q.kpad, bbox);
     if (!ok)
       return set_error(BGEMM_ERROR_INTERNAL, 0, i, "tensor map encoding failed for matrix %d", i);
   }
@@ -197,6 +235,12 @@ bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream) {
   p->info.workspace_bytes = t->ws_bytes;
   p->info.device_bytes += t->ws_bytes + total;
   p->info.kernels_per_execute = 2;
+  if (t->pair) {
+    // one CTA pair per cluster slot, never more pairs than tiles
+    const int pairs = std::max(1, std::min(t->clusters, std::max(p->n_items, 1)));
+    p->grid = 2 * pairs;
+    p->info.grid = p->grid;
+  }
   return BGEMM_SUCCESS;
 }
 
@@ -210,7 +254,8 @@ bgemm_status_t tc_execute(bgemm_plan_s* p, float alpha, const float* const* dA,
   if (e != cudaSuccess) return cuda_error(e, "split/pack launch");
   TcGemmParams gp{p->d_descs, p->d_items, p->n_items, p->d_counters, t->d_tmaps, alpha, beta,
                   dC, t->d_err, 2000000000ull};
-  e = tc_gemm_launch(t->kind, t->split, gp, p->grid, stream);
+  e = t->pair ? tc2_gemm_launch(t->kind, gp, p->grid, stream)
+              : tc_gemm_launch(t->kind, t->split, gp, p->grid, stream);
   if (e != cudaSuccess) return cuda_error(e, "tcgen05 GEMM launch");
   return BGEMM_SUCCESS;
 }
