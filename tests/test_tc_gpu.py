@@ -121,14 +121,32 @@ def test_beta_zero_nan_c_and_k_zero(cuda, mode):
     run_mode(mode, [4, 0, 9, 5], [6, 3, 0, 5], [0, 4, 4, 0], 1.0, 0.5)
 
 
-@pytest.mark.parametrize("cfg", range(8))
+@pytest.mark.parametrize("cfg", [c for c in range(16) if c < 8 or (c & 3) != 3])
 def test_every_tile_config(cuda, cfg):
+    """One-SM tiles (ids 0-7) and CTA-pair tiles (ids 8-14, cta_group::2)."""
     rng = np.random.default_rng(cfg + 50)
-    M = rng.integers(1, 400, 10).tolist()
-    N = rng.integers(1, 400, 10).tolist()
+    M = rng.integers(1, 600, 10).tolist()
+    N = rng.integers(1, 600, 10).tolist()
     K = rng.integers(1, 200, 10).tolist()
     for mode in ("tf32x3", "bf16x3"):
         run_mode(mode, M, N, K, 1.0, 0.25, force=cfg, seed=cfg)
+    if cfg < 8:
+        run_mode("tf32", M, N, K, 0.5, 0.0, force=cfg, seed=cfg)
+
+
+def test_pair_tiles_rejected_for_single_product(cuda):
+    with pytest.raises(bg.BgemmError):
+        bg.Plan([300], [300], [300], [300], [300], [300], mode="tf32", force_tile_config=9)
+
+
+def test_pair_mode_chosen_for_large_matrices(cuda):
+    M = [512, 700, 1024, 33]
+    p = bg.Plan(M, M, M, M, M, M, mode="tf32x3")
+    info = p.info()
+    p.close()
+    assert sum(info["tile_config_hist"][8:]) == 4, info
+    assert info["grid"] % 2 == 0
+    run_mode("tf32x3", M, M, M, 1.0, 0.0, seed=12)
 
 
 def test_small_m_swapped_orientation(cuda):
