@@ -19,8 +19,10 @@ def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--mode", default="tf32x3")
     ap.add_argument("--workload", default="skewed",
-                    choices=["skewed", "plain", "scale", "uneven"])
-    ap.add_argument("--n", type=int, default=400)
+                    choices=["skewed", "plain", "scale", "uneven", "cube"])
+    ap.add_argument("--n", type=int, default=400, help="matrices (skewed, cube)")
+    ap.add_argument("--size", type=int, default=1024, help="M = N = K of the cube workload")
+    ap.add_argument("--force", type=int, default=-1, help="tile configuration id")
     ap.add_argument("--reps", type=int, default=3)
     a = ap.parse_args()
     import torch
@@ -31,11 +33,14 @@ def main() -> None:
     bg.lib()
     if a.workload == "skewed":
         w = workloads.skewed(0, a.n)
+    elif a.workload == "cube":
+        w = workloads.Workload("cube_%d_x%d" % (a.size, a.n), [a.size] * a.n, [a.size] * a.n,
+                               [a.size] * a.n, 1.0, 0.0, "normal")
     else:
         w = {"plain": workloads.plain_fp32, "scale": workloads.simt_at_scale,
              "uneven": workloads.uneven_m}[a.workload](0)
     db = DeviceBatch(w.M, w.N, w.K).fill_fast(w.dist, 0)
-    p = db.plan(a.mode)
+    p = db.plan(a.mode, force_tile_config=a.force)
     for _ in range(a.reps):
         db.execute(p, w.alpha, w.beta)
     torch.cuda.synchronize()
