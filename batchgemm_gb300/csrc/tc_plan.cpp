@@ -10,6 +10,7 @@
 
 #include "plan_internal.h"
 #include "tc_common.h"
+#include "tile_table.h"
 
 namespace bgemm {
 
@@ -33,27 +34,23 @@ struct TcPlan {
 
 static inline long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
 
-// tensor-pipe rate of one SM, flops per ns (TF32: 4096 flops/clk at ~1.9 GHz)
-static double g_rate_ns = 7782.0;
-static int g_nprod = 3;
-static int g_kind = kKindTF32;
+static int g_mode = BGEMM_MODE_TF32X3;
 static bool g_pair = false;
 
-// Modelled tile time: a fixed part plus the MMA time of K, where MMAs
-// narrower than 64 columns cost as much as 64 (operand reads dominate).  A
-// CTA-pair tile runs on two SMs at once.  Only the configurations of the
-// plan's kernel (one-SM or CTA-pair) are offered.
+// Tile time from the (autotuned) cost table of the mode.  Only the
+// configurations of the plan's kernel (one-SM or CTA-pair) are offered.
 static bool tc_eval(int c, int M, int N, int K, long long* tiles, double* t_tile) {
   if (tc_cfg_pair(c) != g_pair) return false;
   if (g_pair && !tc2_cfg_valid(c)) return false;
+  const TileCost& tc = kTcCost[g_mode - 1][c];
+  if (tc.b_ns <= 0.0f) return false;
   const bool swap = tc_cfg_swap(c);
   const int bm = g_pair ? 256 : kTcBM;
   const int bn = g_pair ? tc2_cfg_bn(c) : tc_cfg_bn(c);
   const long long ra = swap ? N : M, rb = swap ? M : N;
   if (cdiv(ra, bm) > 65535 || cdiv(rb, bn) > 65535) return false;
   *tiles = cdiv(ra, bm) * cdiv(rb, bn);
-  const double rate = g_rate_ns * (g_kind == kKindBF16 ? 2.0 : 1.0) * (g_pair ? 2.0 : 1.0);
-  *t_tile = 1200.0 + 2.0 * bm * std::max(bn, 64) * g_nprod * (double)K / rate;
+  *t_tile = tc.a_ns + tc.b_ns * (double)K;
   return true;
 }
 
@@ -93,8 +90,7 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
   }
   static std::mutex mu;
   std::lock_guard<std::mutex> lk(mu);
-  g_nprod = t->nprod;
-  g_kind = t->kind;
+  g_mode = p->mode;
   g_pair = t->pair;
   const int slots = t->pair ? t->clusters : p->facts.num_sms * p->facts.tc_ctas_per_sm;
   return choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, slots, opt, mp);

@@ -1,13 +1,14 @@
-// tile_table.h -- per-tile cost model consumed by the planner.
+// tile_table.h -- per-tile cost model consumed by the planners.
 //
 // Time of one work item of configuration c on a matrix with inner dimension
-// K is modelled as  t = a_c + b_c * K  (nanoseconds, one CTA, with the CTAs
-// that share its SM busy too).  The planner picks, per matrix, the
-// configuration with the least total time and then splits the largest tiles
-// until no single tile is longer than the average load of one persistent
-// CTA (the parallelism rebalance).  tile_table_tuned.inc, written by
-// batchgemm_gb300/autotune.py from measurements on the GPU, overrides the
-// defaults below when present.
+// K is modelled as  t = a_c + b_c * K  (nanoseconds for the CTA -- or CTA
+// pair -- that runs it, with every other persistent CTA busy too).  The
+// planner picks, per matrix, the configuration with the least total time and
+// then splits the largest tiles until no single tile is longer than the
+// average load of one persistent CTA (the parallelism rebalance).
+//
+// tile_table_tuned.inc, written by batchgemm_gb300/autotune.py from
+// measurements on the GPU, replaces the defaults below when present.
 #pragma once
 
 namespace bgemm {
@@ -17,17 +18,44 @@ struct TileCost {
   float b_ns;  // cost per unit of K
 };
 
+// Tensor-core cost tables are indexed [mode - 1][cfg]: TF32, TF32X3, BF16X3;
+// cfg 0..7 one-SM tiles, 8..15 CTA-pair tiles.  b = 0 marks a configuration
+// the mode does not run.
 #if defined(BGEMM_HAVE_TUNED_TABLE)
 #include "tile_table_tuned.inc"
 #else
-// Defaults from a first-principles model: 2 CTAs per SM share 128 FP32
-// lanes at ~1.9 GHz, b = BM*BN / (64 lanes * 1.9 GHz) / efficiency.
+// Defaults from a first-principles model.  SIMT: 2 CTAs per SM share 128
+// FP32 lanes at ~1.9 GHz, b = BM*BN / (64 lanes * 1.9 GHz) / efficiency.
 constexpr TileCost kSimtCost[8] = {
     {1500.f, 16 * 16 / 64 / 1.9f / 0.20f},    {1600.f, 32 * 32 / 64 / 1.9f / 0.45f},
     {1700.f, 64 * 32 / 64 / 1.9f / 0.60f},    {1700.f, 32 * 64 / 64 / 1.9f / 0.60f},
     {1800.f, 64 * 64 / 64 / 1.9f / 0.70f},    {2000.f, 128 * 64 / 64 / 1.9f / 0.80f},
     {2000.f, 64 * 128 / 64 / 1.9f / 0.80f},   {2200.f, 128 * 128 / 64 / 1.9f / 0.85f},
 };
+// Tensor cores: per 128-byte K slice a tile streams its operands from L2,
+// which bounds the narrow tiles, so a tile costs at least what a 128-wide
+// (one SM) or 256-wide (pair) tile costs for the same K.  TF32 runs 4096
+// flops/clk/SM (BF16 8192) at ~1.9 GHz.
+#define BGEMM_TC1(bn, prod, rate) {1500.f, 2.f * 128 * ((bn) > 128 ? (bn) : 128) * (prod) / (rate)}
+#define BGEMM_TC2(bn, prod, rate) {2500.f, 2.f * 256 * (0.6f * 256 + 0.4f * (bn)) * (prod) / (2 * (rate))}
+#define BGEMM_TC_ROW(prod, rate, pairs)                                                          \
+  {BGEMM_TC1(16, prod, rate), BGEMM_TC1(32, prod, rate), BGEMM_TC1(64, prod, rate),             \
+   BGEMM_TC1(128, prod, rate), BGEMM_TC1(16, prod, rate), BGEMM_TC1(32, prod, rate),            \
+   BGEMM_TC1(64, prod, rate), BGEMM_TC1(128, prod, rate),                                        \
+   pairs ? TileCost BGEMM_TC2(64, prod, rate) : TileCost{0.f, 0.f},                              \
+   pairs ? TileCost BGEMM_TC2(128, prod, rate) : TileCost{0.f, 0.f},                             \
+   pairs ? TileCost BGEMM_TC2(256, prod, rate) : TileCost{0.f, 0.f}, TileCost{0.f, 0.f},         \
+   pairs ? TileCost BGEMM_TC2(64, prod, rate) : TileCost{0.f, 0.f},                              \
+   pairs ? TileCost BGEMM_TC2(128, prod, rate) : TileCost{0.f, 0.f},                             \
+   pairs ? TileCost BGEMM_TC2(256, prod, rate) : TileCost{0.f, 0.f}, TileCost{0.f, 0.f}}
+constexpr TileCost kTcCost[3][16] = {
+    BGEMM_TC_ROW(1, 7782.f, false),
+    BGEMM_TC_ROW(3, 7782.f, true),
+    BGEMM_TC_ROW(3, 15564.f, true),
+};
+#undef BGEMM_TC_ROW
+#undef BGEMM_TC2
+#undef BGEMM_TC1
 #endif
 
 }  // namespace bgemm
