@@ -54,18 +54,6 @@ static bool tc_eval(int c, int M, int N, int K, long long* tiles, double* t_tile
   return true;
 }
 
-// CTA pairs pay off when most of the work sits in matrices large enough to
-// fill 256-row tiles.
-static bool want_pairs(const int* M, const int* N, const int* K, int batch) {
-  double big = 0, all = 0;
-  for (int i = 0; i < batch; ++i) {
-    const double f = (double)M[i] * N[i] * K[i];
-    all += f;
-    if (std::max(M[i], N[i]) >= 256 && std::min(M[i], N[i]) >= 64) big += f;
-  }
-  return all > 0 && big >= 0.5 * all;
-}
-
 bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int* K, int batch,
                          const bgemm_plan_options_t* opt, std::vector<MatPlan>& mp) {
   auto* t = new TcPlan();
@@ -76,7 +64,7 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
   if (opt && opt->force_tile_config >= 0)
     t->pair = tc_cfg_pair(opt->force_tile_config);
   else
-    t->pair = t->split && want_pairs(M, N, K, batch);
+    t->pair = t->split;  // candidate; the cost comparison below decides
   if (t->pair && !t->split)
     return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1,
                      "CTA-pair tiles serve the split modes only");
@@ -91,8 +79,34 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
   static std::mutex mu;
   std::lock_guard<std::mutex> lk(mu);
   g_mode = p->mode;
+  const int single_slots = p->facts.num_sms * p->facts.tc_ctas_per_sm;
+  const bool forced = opt && opt->force_tile_config >= 0;
+  if (!forced && t->split && t->clusters > 0) {
+    // plan both kernels with the cost table and keep the shorter makespan
+    auto makespan = [&](const std::vector<MatPlan>& v, int slots) {
+      double total = 0, longest = 0;
+      for (const MatPlan& m : v)
+        if (m.cfg >= 0) {
+          total += (double)m.tiles * m.t_tile;
+          longest = std::max(longest, m.t_tile);
+        }
+      return std::max(total / slots, longest);
+    };
+    std::vector<MatPlan> one, two;
+    g_pair = false;
+    bgemm_status_t s1 = choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, single_slots, opt, one);
+    g_pair = true;
+    bgemm_status_t s2 = choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, t->clusters, opt, two);
+    if (s1 != BGEMM_SUCCESS && s2 != BGEMM_SUCCESS) return s1;
+    const bool pair = s2 == BGEMM_SUCCESS &&
+                      (s1 != BGEMM_SUCCESS ||
+                       makespan(two, t->clusters) < makespan(one, single_slots));
+    t->pair = pair;
+    mp = pair ? two : one;
+    return BGEMM_SUCCESS;
+  }
   g_pair = t->pair;
-  const int slots = t->pair ? t->clusters : p->facts.num_sms * p->facts.tc_ctas_per_sm;
+  const int slots = t->pair ? t->clusters : single_slots;
   return choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, slots, opt, mp);
 }
 
