@@ -140,7 +140,8 @@ def test_framework_rejects_oversized_on_device(cuda):
     db = DeviceBatch([8, 8], [8, 8], [8, 8]).fill()
     before = db.c(1).clone()
     dM = dev([8, 600])  # 600 > max_dim: skipped and reported
-    bg.framework_gemm(dM.data_ptr(), dev([8, 8]).data_ptr(), dev([8, 8]).data_ptr(),
+    dN, dK = dev([8, 8]), dev([8, 8])
+    bg.framework_gemm(dM.data_ptr(), dN.data_ptr(), dK.data_ptr(),
                       db.pA.data_ptr(), db.pB.data_ptr(), db.pC.data_ptr(), 2, 64)
     with pytest.raises(bg.BgemmError):
         bg.framework_check_device()

@@ -140,13 +140,19 @@ def test_pair_tiles_rejected_for_single_product(cuda):
 
 
 def test_pair_mode_chosen_for_large_matrices(cuda):
-    M = [512, 700, 1024, 33]
+    # many large matrices: the cost table prefers 256-row CTA-pair tiles
+    M = [1024] * 48 + [700, 512, 33]
     p = bg.Plan(M, M, M, M, M, M, mode="tf32x3")
     info = p.info()
     p.close()
-    assert sum(info["tile_config_hist"][8:]) == 4, info
+    assert sum(info["tile_config_hist"][8:]) == len(M), info
     assert info["grid"] % 2 == 0
-    run_mode("tf32x3", M, M, M, 1.0, 0.0, seed=12)
+    # few matrices: one-SM tiles give more parallelism
+    few = [512, 700, 1024, 33]
+    p = bg.Plan(few, few, few, few, few, few, mode="tf32x3")
+    assert sum(p.info()["tile_config_hist"][:8]) == 4
+    p.close()
+    run_mode("tf32x3", M[-4:], M[-4:], M[-4:], 1.0, 0.0, seed=12)
 
 
 def test_small_m_swapped_orientation(cuda):
