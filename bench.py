@@ -77,6 +77,13 @@ def max_over_ranks(x, world, device):
     return float(t.item())
 
 
+def whole_job_tflops(flops_per_rank, ms_per_rank, world, device="cpu"):
+    """Replicas: every rank runs the same batch; the job's throughput is all
+    ranks' work over the slowest rank's time."""
+    ms_max = max_over_ranks(ms_per_rank, world, device)
+    return world * flops_per_rank / (ms_max * 1e-3) / 1e12, ms_max
+
+
 # ---------------------------------------------------------------- clocks --
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
@@ -280,8 +287,7 @@ def gpu_leg(args, rank, world, local):
 
     out = {}
     plan, info, ms, clocks = time_mode(args.mode, args.steps, args.warmup, sample_clocks=True)
-    ms_max = max_over_ranks(ms, world, dev)
-    value = world * flops / (ms_max * 1e-3) / 1e12
+    value, ms_max = whole_job_tflops(flops, ms, world, dev)
     err_max, err_mean, nsamp = fp64_sampled_error(db)
     launches_per_step = 1 if args.mode == "simt" else 3
     out.update(value=value, ms=ms_max, info=info, clocks=clocks, err=(err_max, err_mean, nsamp),
