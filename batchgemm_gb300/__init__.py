@@ -90,6 +90,7 @@ def lib() -> ctypes.CDLL:
     L.bgemm_plan_destroy.argtypes = [vp]
     L.bgemm_framework_gemm.argtypes = [vp, vp, vp, vp, vp, vp, vp, i, i, vp]
     L.bgemm_framework_check_device.argtypes = [vp]
+    L.bgemm_framework_gemm_noalloc.argtypes = [vp, vp, vp, vp, vp, vp, i, i, vp, vp]
     L.bgemm_last_error_arg.argtypes = [ip]
     L.bgemm_last_error_arg.restype = i
     L.bgemm_last_error_message.restype = ctypes.c_char_p
@@ -100,7 +101,7 @@ def lib() -> ctypes.CDLL:
     for name in ("bgemm_sgemm_vbatched", "bgemm_plan_create", "bgemm_plan_create_ex",
                  "bgemm_plan_execute", "bgemm_plan_info", "bgemm_plan_check_device",
                  "bgemm_plan_destroy", "bgemm_framework_gemm", "bgemm_framework_check_device",
-                 "bgemm_device_info"):
+                 "bgemm_framework_gemm_noalloc", "bgemm_device_info"):
         getattr(L, name).restype = i
     _lib = L
     return L

@@ -184,6 +184,61 @@ extern "C" bgemm_status_t bgemm_framework_gemm(const int* dM, const int* dN, con
   return BGEMM_SUCCESS;
 }
 
+namespace bgemm {
+
+// Runs the three launches of the device-queue path on scratch the caller
+// provides: `base` holds counters, descriptors, per-matrix queue offsets and
+// up to `cap_items` work items for up to `cap_batch` matrices (layout below,
+// fw_scratch_bytes gives its size); `err` receives bit 0 for a size that is
+// negative or above max_dim.  Allocates nothing.
+size_t fw_scratch_bytes(size_t cap_batch, size_t cap_items) {
+  const size_t off_descs = 256;
+  const size_t off_start = off_descs + ((sizeof(MatDesc) * cap_batch + 255) & ~size_t(255));
+  const size_t off_items = off_start + ((sizeof(int) * cap_batch + 255) & ~size_t(255));
+  return off_items + sizeof(TileItem) * cap_items;
+}
+
+cudaError_t fw_launch_on_scratch(const int* dM, const int* dN, const int* dK, float* const* dA,
+                                 float* const* dB, float* const* dC, int batch, int max_dim,
+                                 void* base, size_t cap_batch, int* err, int grid,
+                                 cudaStream_t stream) {
+  const size_t off_descs = 256;
+  const size_t off_start = off_descs + ((sizeof(MatDesc) * cap_batch + 255) & ~size_t(255));
+  const size_t off_items = off_start + ((sizeof(int) * cap_batch + 255) & ~size_t(255));
+  char* b = static_cast<char*>(base);
+  FwScratch s;
+  s.err = err;
+  s.n_items = reinterpret_cast<int*>(b + 4);
+  s.counters = reinterpret_cast<int*>(b + 128);
+  s.descs = reinterpret_cast<MatDesc*>(b + off_descs);
+  s.mat_start = reinterpret_cast<int*>(b + off_start);
+  s.items = reinterpret_cast<TileItem*>(b + off_items);
+  {
+    std::lock_guard<std::mutex> lk(g_fw_mu);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    FwContext& ctx = g_fw[dev];
+    if (!ctx.consts) {
+      e = cudaMemcpyToSymbol(c_cfgs, kSimtCfgs, sizeof(kSimtCfgs));
+      if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_cost, kSimtCost, sizeof(kSimtCost));
+      if (e != cudaSuccess) return e;
+      ctx.consts = true;
+    }
+  }
+  fw_plan_kernel<<<1, 1024, 0, stream>>>(dM, dN, dK, batch, max_dim, s);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  fw_expand_kernel<<<(batch + 7) / 8, 256, 0, stream>>>(batch, s);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  SimtParams sp{s.descs, s.items, 0, s.n_items, s.counters, 1.0f, 1.0f,
+                const_cast<const float* const*>(dA), const_cast<const float* const*>(dB), dC};
+  return simt_launch(sp, grid, stream);
+}
+
+}  // namespace bgemm
+
 extern "C" bgemm_status_t bgemm_framework_check_device(bgemm_stream_t stream) {
   int dev = 0;
   cudaGetDevice(&dev);

@@ -147,6 +147,28 @@ bgemm_status_t bgemm_framework_gemm(const int* dM, const int* dN,
                                     bgemm_stream_t stream);
 bgemm_status_t bgemm_framework_check_device(bgemm_stream_t stream);
 
+/* --- allocation-free variant of bgemm_framework_gemm ----------------------
+ * No counterpart in the reference.  Same arguments and result as
+ * bgemm_framework_gemm (device size arrays, C_i += A_i*B_i, FP32 SIMT,
+ * bit-exact), for callers that cannot allocate device memory while they run:
+ * a stream under CUDA-graph capture, a real-time loop, a plug-in whose host
+ * application owns the memory budget.  The tile queue lives in a fixed
+ * __device__ array inside the library (about 2.2 MB per device, held until
+ * the process exits) instead of library-allocated memory, so the call never
+ * calls cudaMalloc or cudaFree.  Limits: batch <= 4096 and
+ * batch * ceil(max_dim/16)^2 <= 262144; larger calls return
+ * BGEMM_ERROR_NOT_SUPPORTED.  d_info (device int, may be NULL) receives
+ * bit 0 when a matrix size was negative or above max_dim (that matrix is
+ * skipped); the caller clears it.  The first call on a device looks up the
+ * array's address and should come before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race and must be ordered
+ * by the caller. */
+bgemm_status_t bgemm_framework_gemm_noalloc(const int* dM, const int* dN,
+                                            const int* dK, float* const* dA,
+                                            float* const* dB, float* const* dC,
+                                            int batch, int max_dim, int* d_info,
+                                            bgemm_stream_t stream);
+
 /* --- errors and device facts --------------------------------------------- */
 /* 1-based position of the first invalid argument of the last failing call on
  * this host thread (BLAS convention), 0 if none; for per-matrix arrays the
