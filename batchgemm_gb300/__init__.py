@@ -87,6 +87,7 @@ def lib() -> ctypes.CDLL:
     L.bgemm_plan_execute.argtypes = [vp, f, vp, vp, f, vp, vp]
     L.bgemm_plan_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
     L.bgemm_plan_check_device.argtypes = [vp, vp]
+    L.bgemm_plan_set_kernel_events.argtypes = [vp, vp, vp]
     L.bgemm_plan_destroy.argtypes = [vp]
     L.bgemm_framework_gemm.argtypes = [vp, vp, vp, vp, vp, vp, vp, i, i, vp]
     L.bgemm_framework_check_device.argtypes = [vp]
@@ -101,7 +102,8 @@ def lib() -> ctypes.CDLL:
     for name in ("bgemm_sgemm_vbatched", "bgemm_plan_create", "bgemm_plan_create_ex",
                  "bgemm_plan_execute", "bgemm_plan_info", "bgemm_plan_check_device",
                  "bgemm_plan_destroy", "bgemm_framework_gemm", "bgemm_framework_check_device",
-                 "bgemm_framework_gemm_noalloc", "bgemm_device_info"):
+                 "bgemm_framework_gemm_noalloc", "bgemm_device_info",
+                 "bgemm_plan_set_kernel_events"):
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -167,6 +169,13 @@ class Plan:
 
     def check_device(self, stream=None) -> None:
         _check(lib().bgemm_plan_check_device(self._h, _stream(stream)))
+
+    def set_kernel_events(self, start=None, stop=None) -> None:
+        """Record these torch.cuda.Event objects around the plan's GEMM kernel
+        in every following execute (they must have been recorded once, so that
+        the CUDA event exists)."""
+        h = lambda e: None if e is None else (e.cuda_event or None)
+        _check(lib().bgemm_plan_set_kernel_events(self._h, h(start), h(stop)))
 
     def close(self) -> None:
         if self._h:

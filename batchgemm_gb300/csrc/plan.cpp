@@ -395,7 +395,9 @@ bgemm_status_t plan_execute(bgemm_plan_t p, float alpha, const float* const* dA,
   if (!dC) return set_error(BGEMM_ERROR_INVALID_VALUE, 6, -1, "dC is NULL");
   if (p->mode == BGEMM_MODE_SIMT_FP32) {
     SimtParams sp{p->d_descs, p->d_items, p->n_items, nullptr, p->d_counters, alpha, beta, dA, dB, dC};
+    if (p->ev_start) cudaEventRecord(p->ev_start, stream);
     cudaError_t e = simt_launch(sp, p->grid, stream);
+    if (p->ev_stop) cudaEventRecord(p->ev_stop, stream);
     if (e != cudaSuccess) return cuda_error(e, "SIMT launch");
     return BGEMM_SUCCESS;
   }
@@ -539,6 +541,14 @@ bgemm_status_t bgemm_plan_info(bgemm_plan_t plan, bgemm_plan_info_t* info) {
   if (!plan) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
   if (!info) return set_error(BGEMM_ERROR_INVALID_VALUE, 2, -1, "info is NULL");
   *info = plan->info;
+  return BGEMM_SUCCESS;
+}
+
+bgemm_status_t bgemm_plan_set_kernel_events(bgemm_plan_t plan, void* ev_start, void* ev_stop) {
+  clear_error();
+  if (!plan) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
+  plan->ev_start = static_cast<cudaEvent_t>(ev_start);
+  plan->ev_stop = static_cast<cudaEvent_t>(ev_stop);
   return BGEMM_SUCCESS;
 }
 

@@ -46,6 +46,8 @@ struct bgemm_plan_s {
   bgemm::TcPlan* tc = nullptr;
   std::vector<bgemm::MatDesc> host_descs;
   bgemm_plan_info_t info{};
+  cudaEvent_t ev_start = nullptr;  // profiling hook around the GEMM launch
+  cudaEvent_t ev_stop = nullptr;
 };
 
 namespace bgemm {

@@ -264,8 +264,10 @@ bgemm_status_t tc_execute(bgemm_plan_s* p, float alpha, const float* const* dA,
   if (e != cudaSuccess) return cuda_error(e, "split/pack launch");
   TcGemmParams gp{p->d_descs, p->d_items, p->n_items, p->d_counters, t->d_tmaps, alpha, beta,
                   dC, t->d_err, 2000000000ull};
+  if (p->ev_start) cudaEventRecord(p->ev_start, stream);
   e = t->pair ? tc2_gemm_launch(t->kind, gp, p->grid, stream)
               : tc_gemm_launch(t->kind, t->split, gp, p->grid, stream);
+  if (p->ev_stop) cudaEventRecord(p->ev_stop, stream);
   if (e != cudaSuccess) return cuda_error(e, "tcgen05 GEMM launch");
   return BGEMM_SUCCESS;
 }

@@ -142,6 +142,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def ncu_traffic(mode, workload):
+    """DRAM bytes (read + write) of one launch of the dominant kernel, from the
+    ncu capture summarised in profiles/ncu_traffic.txt (lines:
+    `<mode> <workload> <bytes_per_launch> <how>`); None if not captured."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        p = line.split(None, 3)
+        if len(p) >= 3 and p[0] == mode and p[1] == workload:
+            try:
+                return int(float(p[2]))
+            except ValueError:
+                return None
+    return None
+
+
 # ------------------------------------------------------------ CPU oracle --
 def cpu_sample(w, budget_s=15.0, threads=None):
     """Times the CPU FP32 loop (the oracle port; the reference ships no CPU
@@ -150,28 +167,17 @@ def cpu_sample(w, budget_s=15.0, threads=None):
     import oracle
     threads = threads or os.cpu_count() or 1
     rng = np.random.default_rng(123)
-    order = rng.permutation(w.batch)
-    # grow the sample until it holds ~budget_s of work at a probe rate
-    probe = [i for i in order[:64]]
-    chosen, fl = [], 0.0
-    rate = None
-    for attempt in range(2):
-        if rate is None:
-            target = 2e9  # first probe: ~2 GFLOP
-        else:
-            target = rate * budget_s
-        chosen, fl = [], 0.0
-        for i in order:
-            f = 2.0 * w.M[i] * w.N[i] * w.K[i]
-            if fl + f > target and chosen:
-                continue
-            chosen.append(int(i))
-            fl += f
-            if fl >= target:
-                break
-        Ms = [w.M[i] for i in chosen]
-        Ns = [w.N[i] for i in chosen]
-        Ks = [w.K[i] for i in chosen]
+    order = [int(i) for i in rng.permutation(w.batch)]
+    # whole matrices in random order, in chunks of growing size, until the
+    # timed CPU work reaches the budget (data generation is not timed)
+    fl_total, t_total, n_done, used, pos, chunk = 0.0, 0.0, 0, 1, 0, 8
+    while t_total < budget_s and pos < len(order):
+        sel = order[pos:pos + chunk]
+        pos += len(sel)
+        chunk *= 2
+        Ms = [w.M[i] for i in sel]
+        Ns = [w.N[i] for i in sel]
+        Ks = [w.K[i] for i in sel]
         As = [rng.standard_normal(max(m * k, 1)).astype(np.float32) for m, k in zip(Ms, Ks)]
         Bs = [rng.standard_normal(max(k * n, 1)).astype(np.float32) for k, n in zip(Ks, Ns)]
         Cs = [np.zeros(max(m * n, 1), np.float32) for m, n in zip(Ms, Ns)]
@@ -179,10 +185,12 @@ def cpu_sample(w, budget_s=15.0, threads=None):
         used = oracle.vbatched_f32(Ms, Ns, Ks, w.alpha, As, [max(1, m) for m in Ms], Bs,
                                    [max(1, k) for k in Ks], w.beta, Cs, [max(1, m) for m in Ms],
                                    nthreads=threads)
-        dt = time.perf_counter() - t0
-        rate = fl / dt
-    desc = ("%d of %d matrices (%.2f GFLOP, random subset, whole matrices), FP32 fma loop, "
-            "%d threads, %.1f s" % (len(chosen), w.batch, fl / 1e9, used, dt))
+        t_total += time.perf_counter() - t0
+        fl_total += sum(2.0 * m * n * k for m, n, k in zip(Ms, Ns, Ks))
+        n_done += len(sel)
+    rate = fl_total / max(t_total, 1e-9)
+    desc = ("%d of %d matrices (%.1f GFLOP, random order, whole matrices), FP32 fma loop, "
+            "%d threads, %.1f s timed" % (n_done, w.batch, fl_total / 1e9, used, t_total))
     return rate / 1e12, used, desc
 
 
@@ -289,9 +297,25 @@ def gpu_leg(args, rank, world, local):
     plan, info, ms, clocks = time_mode(args.mode, args.steps, args.warmup, sample_clocks=True)
     value, ms_max = whole_job_tflops(flops, ms, world, dev)
     err_max, err_mean, nsamp = fp64_sampled_error(db)
-    launches_per_step = 1 if args.mode == "simt" else 3
     out.update(value=value, ms=ms_max, info=info, clocks=clocks, err=(err_max, err_mean, nsamp),
-               launches=launches_per_step * args.steps)
+               launches=info["kernels_per_execute"] * args.steps)
+    # the dominant (GEMM) kernel alone: events recorded by the library around
+    # its launch, on the stream it is launched on, over `steps` executes
+    evs = []
+    for _ in range(args.steps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        b.record(s)
+        evs.append((a, b))
+    s.synchronize()
+    with torch.cuda.stream(s):
+        for a, b in evs:
+            plan.set_kernel_events(a, b)
+            db.execute(plan, w.alpha, w.beta, stream=s)
+    s.synchronize()
+    plan.set_kernel_events(None, None)
+    out["kernel_ms"] = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
     plan.close()
 
     # other modes on the same batch (a few steps each)
@@ -311,28 +335,37 @@ def gpu_leg(args, rank, world, local):
                 extra[mode] = {"unavailable": e.message}
     out["extra"] = extra
 
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel: algorithmic flops of one launch over its
+    # own CUDA-event duration (pack pre-pass excluded; it is HBM-bound and
+    # reported separately as pre_pass_ms)
     mode = args.mode
+    kms = out["kernel_ms"]
     clk_max = (clocks or {}).get("sm_max_mhz") or 2070.0
+    traffic = ncu_traffic(mode, w.name)
     if mode == "simt":
         peak = num_sms * 128 * 2 * clk_max * 1e6 / 1e12
-        out["roofline"] = {"bound": "fp32_simt", "achieved": round(value / world, 3),
+        ach = flops / (kms * 1e-3) / 1e12
+        out["roofline"] = {"bound": "fp32_simt", "achieved": round(ach, 3),
                            "peak": round(peak, 2), "unit": "TFLOP/s",
-                           "frac": round(value / world / peak, 4), "traffic": None,
-                           "peak_source": "SMs x 128 FP32 lanes x 2 x max SM clock (of device "
-                                          "properties; no measured FP32 peak)"}
+                           "frac": round(ach / peak, 4), "traffic": traffic,
+                           "kernel": "simt_persistent_kernel", "kernel_ms": round(kms, 4),
+                           "algorithmic_flops_per_launch": flops,
+                           "peak_source": "SMs x 128 FP32 lanes x 2 x max SM clock (device "
+                                          "properties; MEASURED_PEAKS.json has no FP32 figure)"}
     else:
         bf16 = peaks.get("bf16_tflops", 1900.0)
         src = "of measured" if "bf16_tflops" in peaks else "of fallback"
-        tf32_peak = bf16 / 2.0
         mult = 3.0 if mode in ("tf32x3", "bf16x3") else 1.0
-        pipe_peak = bf16 if mode == "bf16x3" else tf32_peak
-        pipe = mult * value / world
-        out["roofline"] = {"bound": "tensor", "achieved": round(pipe, 2),
+        pipe_peak = bf16 if mode == "bf16x3" else bf16 / 2.0
+        ach = mult * flops / (kms * 1e-3) / 1e12
+        out["roofline"] = {"bound": "tensor", "achieved": round(ach, 2),
                            "peak": round(pipe_peak, 1), "unit": "TFLOP/s",
-                           "frac": round(pipe / pipe_peak, 4), "traffic": None,
-                           "peak_source": "%s bf16 dense %s%s" % (
-                               src, "" if mode == "bf16x3" else "/ 2 (TF32 rate)",
+                           "frac": round(ach / pipe_peak, 4), "traffic": traffic,
+                           "kernel": "tc2_gemm_kernel / tc_gemm_kernel", "kernel_ms": round(kms, 4),
+                           "pre_pass_ms": round(out["ms"] - kms, 4),
+                           "algorithmic_flops_per_launch": mult * flops,
+                           "peak_source": "%s bf16 dense%s%s" % (
+                               src, "" if mode == "bf16x3" else " / 2 (TF32 rate)",
                                "; achieved counts the 3 tensor products" if mult > 1 else "")}
 
     # end to end through the one-shot C-ABI call with host buffers

@@ -123,6 +123,14 @@ bgemm_status_t bgemm_plan_execute(bgemm_plan_t plan, float alpha,
                                   const float* const* dB, float beta,
                                   float* const* dC, bgemm_stream_t stream);
 bgemm_status_t bgemm_plan_info(bgemm_plan_t plan, bgemm_plan_info_t* info);
+/* Profiling hook (no counterpart in the reference, which brackets its whole
+ * launch loop with events, CUDA/framework/gemm.cu:203-214): every following
+ * bgemm_plan_execute records ev_start / ev_stop (cudaEvent_t; either may be
+ * NULL) on its stream immediately before and after the plan's GEMM kernel,
+ * so the kernel's own duration can be read with cudaEventElapsedTime.
+ * Pass NULL, NULL to stop. */
+bgemm_status_t bgemm_plan_set_kernel_events(bgemm_plan_t plan, void* ev_start,
+                                            void* ev_stop);
 /* Blocks until the plan's previous launches on `stream` finish and reports
  * BGEMM_ERROR_DEVICE_TIMEOUT if a device-side wait expired in any of them
  * (the flag is then cleared). */
