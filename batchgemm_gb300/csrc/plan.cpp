@@ -599,6 +599,14 @@ bgemm_status_t bgemm_device_info(int* num_sms, int* simt_ctas_per_sm, int* tc_ct
 
 int bgemm_version(void) { return 100; }
 
+int bgemm_debug_compare_tensor_maps(void* plan, void* stream, int* n_maps, int* n_diff,
+                                    int* first_byte) {
+  clear_error();
+  if (!plan || !n_maps || !n_diff || !first_byte) return -1;
+  return tc_debug_compare_tmaps(static_cast<bgemm_plan_s*>(plan),
+                                static_cast<cudaStream_t>(stream), n_maps, n_diff, first_byte);
+}
+
 int bgemm_debug_simt_queue(const int* M, const int* N, const int* K, int batch, int slots,
                            int force_cfg, int rebalance, int* cfg_out, int* items_out,
                            int max_items) {

@@ -75,6 +75,8 @@ bgemm_status_t tc_execute(bgemm_plan_s* p, float alpha, const float* const* dA,
                           const float* const* dB, float beta, float* const* dC,
                           cudaStream_t stream);
 bgemm_status_t tc_check_device(bgemm_plan_s* p, cudaStream_t stream);
+int tc_debug_compare_tmaps(bgemm_plan_s* p, cudaStream_t stream, int* n_maps, int* n_diff,
+                           int* first_byte);
 void tc_plan_release(bgemm_plan_s* p);
 
 }  // namespace bgemm

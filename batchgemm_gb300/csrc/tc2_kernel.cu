@@ -116,6 +116,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       bool inflight[kS];
       for (int s = 0; s < kS; ++s) inflight[s] = false, inflight_phase[s] = 0;
       bool ok = true;
+      int last_mat = -1;
       for (int t = 0; ok; ++t) {
         const int it = snake(cl, t, ncl);
         if (it >= p.n_items) break;
@@ -124,6 +125,10 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
         const int bn = tc2_cfg_bn(d.cfg);
         const int hb = bn >> 1;
         const CUtensorMap* tm = p.tmaps + 4 * ti.mat;
+        if (ti.mat != last_mat && d.K > 0) {
+          for (int q = 0; q < 4; ++q) tmap_acquire(tm + q);
+          last_mat = ti.mat;
+        }
         const int nk = (d.K + KE - 1) / KE;
         const uint32_t tx = 2u * 2u * (uint32_t)(kA + hb * 128);  // both CTAs, hi + lo
         const int row_a = ti.tm * 256 + (int)rank * kRows;

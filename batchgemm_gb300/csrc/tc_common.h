@@ -67,7 +67,22 @@ struct TcGemmParams {
   unsigned long long timeout_ns;
 };
 
+// Device-side construction of the per-matrix tensor maps: one warp per map
+// patches a host-encoded template (address, dims, row stride, box rows) with
+// tensormap.replace and publishes it with a release fence.
+struct TcTmapParams {
+  const MatDesc* descs;
+  const PackDesc* pdescs;
+  const CUtensorMap* templ;  // any valid map of the plan's element kind
+  CUtensorMap* out;          // 4 per matrix
+  const char* ws;
+  int batch;
+  int kind;
+  int pair;
+};
+
 cudaError_t tc_pack_launch(const TcPackParams& p, int grid, cudaStream_t s);
+cudaError_t tc_tmap_launch(const TcTmapParams& p, cudaStream_t s);
 cudaError_t tc_gemm_launch(int kind, int split, const TcGemmParams& p, int grid, cudaStream_t s);
 int tc_smem_bytes(int kind, int split);
 // CTA-pair kernel (split modes); grid = 2 x clusters

@@ -218,6 +218,42 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
   }
 }
 
+// ------------------------------------------------ per-matrix tensor maps --
+// One warp per map: map j of matrix i = j / 4 is part j % 4 (A-side hi, lo,
+// B-side hi, lo).  The A side is A unless the matrix's configuration swaps
+// the operands; its boxes are 128 rows, the B side's bn rows (bn / 2 per CTA
+// of a pair).
+__global__ void __launch_bounds__(128) tc_tmap_kernel(const TcTmapParams p) {
+  __shared__ __align__(128) CUtensorMap maps[4];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.x * 4 + warp;
+  if (j >= 4 * p.batch) return;
+  const int i = j >> 2, part = j & 3;
+  const MatDesc d = p.descs[i];
+  if (d.M == 0 || d.N == 0 || d.K == 0) return;  // never loaded
+  const PackDesc pd = p.pdescs[i];
+  const bool swap = tc_cfg_swap(d.cfg);
+  const bool a_side = part < 2, lo = part & 1;
+  const bool use_a = a_side != swap;  // which operand's panel this map walks
+  const long long off = use_a ? (lo ? pd.a_lo : pd.a_hi) : (lo ? pd.b_lo : pd.b_hi);
+  const int rows = use_a ? d.M : d.N;
+  const int esz = (p.kind == kKindTF32) ? 4 : 2;
+  const int box = a_side ? kTcBM : (p.pair ? tc2_cfg_bn(d.cfg) / 2 : tc_cfg_bn(d.cfg));
+  uint32_t* dst = reinterpret_cast<uint32_t*>(&maps[warp]);
+  dst[lane] = reinterpret_cast<const uint32_t*>(p.templ)[lane];
+  __syncwarp();
+  const uint32_t sm = smem_u32(&maps[warp]);
+  if (lane == 0) {
+    tmap_set_address(sm, p.ws + off);
+    tmap_set_dim(sm, 0, (uint32_t)d.K);
+    tmap_set_dim(sm, 1, (uint32_t)rows);
+    tmap_set_row_stride(sm, (uint64_t)pd.kpad * esz);
+    tmap_set_box_rows(sm, (uint32_t)box);
+  }
+  __syncwarp();
+  tmap_publish(p.out + j, sm);
+}
+
 // ------------------------------------------------------------- the GEMM --
 template <int KIND, int SPLIT>
 __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams p) {
@@ -294,6 +330,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
         const int bn = tc_cfg_bn(d.cfg);
         const CUtensorMap* tm = p.tmaps + 4 * ti.mat;
         if (ti.mat != last_mat && d.K > 0) {
+          for (int q = 0; q < 4; ++q) tmap_acquire(tm + q);
           prefetch_tmap(tm);
           prefetch_tmap(tm + 2);
           last_mat = ti.mat;
@@ -554,6 +591,12 @@ cudaError_t launch_gemm(const TcGemmParams& p, int grid, cudaStream_t s) {
 }
 
 }  // namespace
+
+cudaError_t tc_tmap_launch(const TcTmapParams& p, cudaStream_t s) {
+  if (p.batch == 0) return cudaSuccess;
+  tc_tmap_kernel<<<p.batch, 128, 0, s>>>(p);  // 4 warps = the 4 maps of one matrix
+  return cudaGetLastError();
+}
 
 cudaError_t tc_pack_launch(const TcPackParams& p, int grid, cudaStream_t s) {
   if (p.n_jobs == 0) return cudaSuccess;

@@ -30,6 +30,7 @@ struct TcPlan {
   int pack_grid = 1;
   bool pair = false;   // CTA-pair kernel (tc2_kernel.cu)
   int clusters = 0;    // CTA pairs resident at once
+  bool host_tmaps = false;  // encode every tensor map on the host (comparison path)
 };
 
 static inline long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
@@ -60,6 +61,7 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
   t->kind = (p->mode == BGEMM_MODE_BF16X3) ? kKindBF16 : kKindTF32;
   t->split = (p->mode == BGEMM_MODE_TF32) ? 0 : 1;
   t->nprod = t->split ? 3 : 1;
+  t->host_tmaps = opt && opt->host_tensor_maps;
   p->tc = t;
   if (opt && opt->force_tile_config >= 0)
     t->pair = tc_cfg_pair(opt->force_tile_config);
@@ -196,7 +198,8 @@ bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream) {
   t->pack_grid = (int)std::max<long long>(1, std::min<long long>(t->n_jobs,
                                                                  (long long)p->facts.num_sms * 8));
 
-  const size_t off_tm = 0;
+  const size_t off_tpl = 0;  // template map for the device-side build
+  const size_t off_tm = off_tpl + sizeof(CUtensorMap) * 2;
   const size_t off_pd = off_tm + sizeof(CUtensorMap) * 4 * (size_t)batch;
   const size_t off_jobs = off_pd + ((sizeof(PackDesc) * (size_t)batch + 255) & ~size_t(255));
   const size_t off_err = off_jobs + ((sizeof(PackJob) * jobs.size() + 255) & ~size_t(255));
@@ -215,7 +218,15 @@ bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream) {
   std::memset(h, 0, total);
   auto* tm = reinterpret_cast<CUtensorMap*>(h + off_tm);
   char* ws = static_cast<char*>(t->d_ws);
-  for (int i = 0; i < batch; ++i) {
+  {
+    // a valid map of the plan's element kind; the device patches one copy per
+    // operand panel (address, dims, row stride, box rows)
+    const int ke = 128 / esz;
+    if (!encode_panel(reinterpret_cast<CUtensorMap*>(h + off_tpl), t->kind, ws, ke, kTcBM, ke,
+                      kTcBM))
+      return set_error(BGEMM_ERROR_INTERNAL, 0, -1, "template tensor map encoding failed");
+  }
+  for (int i = 0; i < batch && t->host_tmaps; ++i) {
     const MatDesc& d = hd[i];
     if (d.M == 0 || d.N == 0 || d.K == 0) continue;
     const bool swap = tc_cfg_swap(d.cfg);
@@ -242,6 +253,13 @@ bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream) {
   t->d_err = reinterpret_cast<int*>(dm + off_err);
   e = cudaMemcpyAsync(t->d_mem, t->h_pin, total, cudaMemcpyHostToDevice, stream);
   if (e != cudaSuccess) return cuda_error(e, "tensor-core descriptor upload");
+  if (!t->host_tmaps) {
+    // per-matrix tensor maps built on the device, once per plan
+    TcTmapParams tp{p->d_descs, t->d_pdescs, reinterpret_cast<CUtensorMap*>(dm + off_tpl),
+                    t->d_tmaps, ws, batch, t->kind, t->pair ? 1 : 0};
+    e = tc_tmap_launch(tp, stream);
+    if (e != cudaSuccess) return cuda_error(e, "tensor-map build launch");
+  }
   p->info.workspace_bytes = t->ws_bytes;
   p->info.device_bytes += t->ws_bytes + total;
   p->info.kernels_per_execute = 2;
@@ -252,6 +270,54 @@ bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream) {
     p->info.grid = p->grid;
   }
   return BGEMM_SUCCESS;
+}
+
+// Host re-encoding of every map the device built, for a byte comparison.
+int tc_debug_compare_tmaps(bgemm_plan_s* p, cudaStream_t stream, int* n_maps, int* n_diff,
+                           int* first_byte) {
+  TcPlan* t = p->tc;
+  if (!t) return -1;
+  if (cudaStreamSynchronize(stream) != cudaSuccess) return -1;
+  const int batch = p->batch;
+  std::vector<CUtensorMap> dev(4 * (size_t)batch), host(4 * (size_t)batch);
+  if (batch > 0 && cudaMemcpy(dev.data(), t->d_tmaps, sizeof(CUtensorMap) * 4 * (size_t)batch,
+                              cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -1;
+  std::vector<PackDesc> pd(batch);
+  if (batch > 0 && cudaMemcpy(pd.data(), t->d_pdescs, sizeof(PackDesc) * (size_t)batch,
+                              cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -1;
+  char* ws = static_cast<char*>(t->d_ws);
+  int maps = 0, diff = 0, first = -1;
+  for (int i = 0; i < batch; ++i) {
+    const MatDesc& d = p->host_descs[i];
+    if (d.M == 0 || d.N == 0 || d.K == 0) continue;
+    const bool swap = tc_cfg_swap(d.cfg);
+    const int bbox = t->pair ? tc2_cfg_bn(d.cfg) / 2 : tc_cfg_bn(d.cfg);
+    const PackDesc& q = pd[i];
+    const long long off[4] = {swap ? q.b_hi : q.a_hi, swap ? q.b_lo : q.a_lo,
+                              swap ? q.a_hi : q.b_hi, swap ? q.a_lo : q.b_lo};
+    const int rows[4] = {swap ? d.N : d.M, swap ? d.N : d.M, swap ? d.M : d.N, swap ? d.M : d.N};
+    for (int part = 0; part < 4; ++part) {
+      CUtensorMap& h = host[4 * i + part];
+      if (!encode_panel(&h, t->kind, ws + off[part], d.K, rows[part], q.kpad,
+                        part < 2 ? kTcBM : bbox))
+        return -1;
+      ++maps;
+      const unsigned char* a = reinterpret_cast<const unsigned char*>(&h);
+      const unsigned char* b = reinterpret_cast<const unsigned char*>(&dev[4 * i + part]);
+      for (int k = 0; k < (int)sizeof(CUtensorMap); ++k)
+        if (a[k] != b[k]) {
+          if (first < 0) first = k;
+          ++diff;
+          break;
+        }
+    }
+  }
+  *n_maps = maps;
+  *n_diff = diff;
+  *first_byte = first;
+  return 0;
 }
 
 bgemm_status_t tc_execute(bgemm_plan_s* p, float alpha, const float* const* dA,

@@ -157,6 +157,55 @@ __device__ __noinline__ bool wait_bounded(uint32_t bar, uint32_t parity, int* er
   }
 }
 
+// ------------------------------------------------- tensor maps on device --
+// Field patches of a 128-byte tensor map held in shared memory (the address
+// operand is the shared address widened to 64 bits).
+__device__ __forceinline__ void tmap_set_address(uint32_t smem_map, const void* gaddr) {
+  const uint64_t a = smem_map;
+  asm volatile("tensormap.replace.tile.global_address.shared::cta.b1024.b64 [%0], %1;" ::"l"(a),
+               "l"(reinterpret_cast<uint64_t>(gaddr))
+               : "memory");
+}
+__device__ __forceinline__ void tmap_set_dim(uint32_t smem_map, int ord, uint32_t v) {
+  const uint64_t a = smem_map;
+  if (ord == 0)
+    asm volatile("tensormap.replace.tile.global_dim.shared::cta.b1024.b32 [%0], 0, %1;" ::"l"(a),
+                 "r"(v)
+                 : "memory");
+  else
+    asm volatile("tensormap.replace.tile.global_dim.shared::cta.b1024.b32 [%0], 1, %1;" ::"l"(a),
+                 "r"(v)
+                 : "memory");
+}
+// Stride of dimension 1 in bytes (ordinal 0: dimension 0 has unit stride).
+__device__ __forceinline__ void tmap_set_row_stride(uint32_t smem_map, uint64_t bytes) {
+  const uint64_t a = smem_map;
+  asm volatile("tensormap.replace.tile.global_stride.shared::cta.b1024.b64 [%0], 0, %1;" ::"l"(a),
+               "l"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tmap_set_box_rows(uint32_t smem_map, uint32_t rows) {
+  const uint64_t a = smem_map;
+  asm volatile("tensormap.replace.tile.box_dim.shared::cta.b1024.b32 [%0], 1, %1;" ::"l"(a),
+               "r"(rows)
+               : "memory");
+}
+// Copy the patched map to global memory, ordered before later uses through
+// the tensor-map proxy (warp-collective).
+__device__ __forceinline__ void tmap_publish(void* gmem_map, uint32_t smem_map) {
+  asm volatile(
+      "tensormap.cp_fenceproxy.global.shared::cta.tensormap::generic.release.gpu.sync.aligned"
+      " [%0], [%1], 128;" ::"l"(reinterpret_cast<uint64_t>(gmem_map)),
+      "r"(smem_map)
+      : "memory");
+}
+// Consumer side: make a map written by another kernel visible to TMA.
+__device__ __forceinline__ void tmap_acquire(const CUtensorMap* map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                   reinterpret_cast<uint64_t>(map))
+               : "memory");
+}
+
 // ------------------------------------------------------ CTA pair (2 SMs) --
 // A cluster of two CTAs on two SMs runs one cta_group::2 UMMA: each CTA holds
 // half of A (its 128 rows of M = 256) and half of B (N/2 rows) in its own

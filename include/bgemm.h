@@ -90,7 +90,9 @@ typedef struct bgemm_plan_options {
   int force_tile_config;    /* -1: heuristic; otherwise a config id of the mode */
   int max_ctas;             /* 0: one wave of persistent CTAs; otherwise a cap  */
   int disable_rebalance;    /* 1: skip the parallelism (wavefront) rebalance    */
-  int reserved[8];
+  int host_tensor_maps;     /* 1: encode the TMA tensor maps on the host instead
+                               of building them on the device (for comparison) */
+  int reserved[7];
 } bgemm_plan_options_t;
 
 /* --- one-shot entry (host size arrays, like CUDA/framework/gemm.cu:39-41) ---

@@ -25,6 +25,14 @@ int bgemm_debug_simt_queue(const int* M, const int* N, const int* K, int batch, 
                            int force_cfg, int rebalance, int* cfg_out, int* items_out,
                            int max_items);
 
+/* Tensor-core plans: waits for `stream`, encodes on the host the tensor maps
+ * that the device built for the plan, and compares them byte by byte.
+ * *n_maps receives the number of maps compared, *n_diff how many differ,
+ * *first_byte the first differing byte of the first differing map (-1 if
+ * none).  Returns 0, or -1 for a non-tensor-core plan. */
+int bgemm_debug_compare_tensor_maps(void* plan, void* stream, int* n_maps, int* n_diff,
+                                    int* first_byte);
+
 #ifdef __cplusplus
 }
 #endif
