@@ -239,8 +239,10 @@ __global__ void __launch_bounds__(128) tc_tmap_kernel(const TcTmapParams p) {
   const int rows = use_a ? d.M : d.N;
   const int esz = (p.kind == kKindTF32) ? 4 : 2;
   const int box = a_side ? kTcBM : (p.pair ? tc2_cfg_bn(d.cfg) / 2 : tc_cfg_bn(d.cfg));
+  const long long extent = (long long)rows * pd.kpad * esz;
+  const CUtensorMap* tpl = p.templ + tmap_template_index(box, extent >= kTmapLargeExtent);
   uint32_t* dst = reinterpret_cast<uint32_t*>(&maps[warp]);
-  dst[lane] = reinterpret_cast<const uint32_t*>(p.templ)[lane];
+  dst[lane] = reinterpret_cast<const uint32_t*>(tpl)[lane];
   __syncwarp();
   const uint32_t sm = smem_u32(&maps[warp]);
   if (lane == 0) {
@@ -248,7 +250,6 @@ __global__ void __launch_bounds__(128) tc_tmap_kernel(const TcTmapParams p) {
     tmap_set_dim(sm, 0, (uint32_t)d.K);
     tmap_set_dim(sm, 1, (uint32_t)rows);
     tmap_set_row_stride(sm, (uint64_t)pd.kpad * esz);
-    tmap_set_box_rows(sm, (uint32_t)box);
   }
   __syncwarp();
   tmap_publish(p.out + j, sm);

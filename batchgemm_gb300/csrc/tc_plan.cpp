@@ -198,8 +198,8 @@ bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream) {
   t->pack_grid = (int)std::max<long long>(1, std::min<long long>(t->n_jobs,
                                                                  (long long)p->facts.num_sms * 8));
 
-  const size_t off_tpl = 0;  // template map for the device-side build
-  const size_t off_tm = off_tpl + sizeof(CUtensorMap) * 2;
+  const size_t off_tpl = 0;  // template maps for the device-side build
+  const size_t off_tm = off_tpl + sizeof(CUtensorMap) * 2 * kTmapBoxClasses;
   const size_t off_pd = off_tm + sizeof(CUtensorMap) * 4 * (size_t)batch;
   const size_t off_jobs = off_pd + ((sizeof(PackDesc) * (size_t)batch + 255) & ~size_t(255));
   const size_t off_err = off_jobs + ((sizeof(PackJob) * jobs.size() + 255) & ~size_t(255));
@@ -219,12 +219,17 @@ bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream) {
   auto* tm = reinterpret_cast<CUtensorMap*>(h + off_tm);
   char* ws = static_cast<char*>(t->d_ws);
   {
-    // a valid map of the plan's element kind; the device patches one copy per
-    // operand panel (address, dims, row stride, box rows)
+    // templates per (box height, extent class); the device patches one copy
+    // per operand panel (address, dims, row stride)
     const int ke = 128 / esz;
-    if (!encode_panel(reinterpret_cast<CUtensorMap*>(h + off_tpl), t->kind, ws, ke, kTcBM, ke,
-                      kTcBM))
-      return set_error(BGEMM_ERROR_INTERNAL, 0, -1, "template tensor map encoding failed");
+    auto* tpl = reinterpret_cast<CUtensorMap*>(h + off_tpl);
+    for (int b = 16; b <= 128; b *= 2) {
+      const bool ok = encode_panel(&tpl[tmap_template_index(b, false)], t->kind, ws, ke, kTcBM, ke,
+                                   b) &&  // 128 rows x 128 B = 16 KiB
+                      encode_panel(&tpl[tmap_template_index(b, true)], t->kind, ws, ke, 1 << 20,
+                                   ke, b);  // 2^20 rows x 128 B = 128 MiB
+      if (!ok) return set_error(BGEMM_ERROR_INTERNAL, 0, -1, "template tensor map encoding failed");
+    }
   }
   for (int i = 0; i < batch && t->host_tmaps; ++i) {
     const MatDesc& d = hd[i];

@@ -184,12 +184,6 @@ __device__ __forceinline__ void tmap_set_row_stride(uint32_t smem_map, uint64_t 
                "l"(bytes)
                : "memory");
 }
-__device__ __forceinline__ void tmap_set_box_rows(uint32_t smem_map, uint32_t rows) {
-  const uint64_t a = smem_map;
-  asm volatile("tensormap.replace.tile.box_dim.shared::cta.b1024.b32 [%0], 1, %1;" ::"l"(a),
-               "r"(rows)
-               : "memory");
-}
 // Copy the patched map to global memory, ordered before later uses through
 // the tensor-map proxy (warp-collective).
 __device__ __forceinline__ void tmap_publish(void* gmem_map, uint32_t smem_map) {

@@ -31,6 +31,31 @@ MODES = {
 }
 
 
+def test_device_tensor_maps_match_host_encoding(cuda):
+    """The tensor maps the device builds are byte-identical to the driver's
+    host encoding of the same panels (runs before any GEMM of this file)."""
+    import ctypes
+    L = bg.lib()
+    L.bgemm_debug_compare_tensor_maps.argtypes = [ctypes.c_void_p] * 2 + \
+        [ctypes.POINTER(ctypes.c_int)] * 3
+    rng = np.random.default_rng(17)
+    # extents on both sides of 128 KiB, K above and below 256, tiny and wide
+    M = [1, 17, 300, 129, 600, 64, 1024, 2000, 40, 5] + rng.integers(1, 3000, 10).tolist()
+    N = [5, 64, 33, 250, 700, 2000, 1024, 3, 41, 4096] + rng.integers(1, 3000, 10).tolist()
+    K = [3, 100, 64, 31, 333, 1, 1024, 2048, 257, 96] + rng.integers(1, 3000, 10).tolist()
+    for mode in ("tf32", "tf32x3", "bf16x3"):
+        forces = [-1, 0, 1, 2, 3, 4, 5, 6, 7] + ([8, 9, 10, 12, 13, 14] if mode != "tf32" else [])
+        for f in forces:
+            p = bg.Plan(M, N, K, M, K, M, mode=mode, force_tile_config=f)
+            a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+            rc = L.bgemm_debug_compare_tensor_maps(p._h, None, ctypes.byref(a), ctypes.byref(b),
+                                                   ctypes.byref(c))
+            p.close()
+            assert rc == 0 and a.value == 4 * len(M), (mode, f, rc, a.value)
+            assert b.value == 0, "%s cfg %d: %d of %d maps differ (first byte %d)" % (
+                mode, f, b.value, a.value, c.value)
+
+
 def split_check(db, host, got, alpha, beta, omode, factor):
     """|c - exact(split products)| <= factor * 2^-24 * sqrt(K) * bound."""
     hA, hB, hC0 = host
