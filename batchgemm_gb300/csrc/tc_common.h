@@ -11,7 +11,10 @@
 namespace bgemm {
 
 // Element kinds of the packed operands.
-enum TcKind : int { kKindTF32 = 0, kKindBF16 = 1 };
+// kKindRaw: the pre-pass only transposes/compacts operands to K-major FP32
+// (4 B per element) and the GEMM splits them in shared memory (3xTF32 on
+// CTA pairs).
+enum TcKind : int { kKindTF32 = 0, kKindBF16 = 1, kKindRaw = 2 };
 
 // Tile configurations: UMMA M = 128 rows of the "A side" operand, UMMA N =
 // BN rows of the "B side".  Ids 0..3 keep A on the A side (BN 16/32/64/128);
@@ -98,5 +101,8 @@ int tc_smem_bytes(int kind, int split);
 // CTA-pair kernel (split modes); grid = 2 x clusters
 cudaError_t tc2_gemm_launch(int kind, const TcGemmParams& p, int grid, cudaStream_t s);
 int tc2_max_clusters();
+// CTA-pair 3xTF32 kernel that splits raw FP32 operands in shared memory
+cudaError_t tc2s_gemm_launch(const TcGemmParams& p, int grid, cudaStream_t s);
+int tc2s_max_clusters();
 
 }  // namespace bgemm

@@ -71,18 +71,11 @@ constexpr int kEpiWarps = 8;
 constexpr int kEpiCols = kTcMaxBN / 2;
 
 // ---------------------------------------------------- operand splitting --
-__device__ __forceinline__ float round_keep(float x, int drop) {
-  uint32_t u = __float_as_uint(x);
-  if ((u & 0x7f800000u) == 0x7f800000u) return x;
-  const uint32_t half = (1u << (drop - 1)) - 1u;
-  u += half + ((u >> drop) & 1u);
-  u &= ~((1u << drop) - 1u);
-  return __uint_as_float(u);
-}
-
 __device__ __forceinline__ void put(char* hi, char* lo, long long idx, float x, int kind,
                                     int split) {
-  if (kind == kKindTF32) {
+  if (kind == kKindRaw) {
+    reinterpret_cast<float*>(hi)[idx] = x;
+  } else if (kind == kKindTF32) {
     const float h = round_keep(x, 13);
     reinterpret_cast<float*>(hi)[idx] = h;
     if (split) {
@@ -104,6 +97,10 @@ __device__ __forceinline__ void put(char* hi, char* lo, long long idx, float x, 
 // 16-byte (TF32) or 8-byte (BF16) store each; idx is a multiple of 4.
 __device__ __forceinline__ void put4(char* hi, char* lo, long long idx, const float* x, int kind,
                                      int split) {
+  if (kind == kKindRaw) {
+    *reinterpret_cast<float4*>(reinterpret_cast<float*>(hi) + idx) = make_float4(x[0], x[1], x[2], x[3]);
+    return;
+  }
   float h[4], l[4];
   const int drop = (kind == kKindTF32) ? 13 : 16;
 #pragma unroll
@@ -237,7 +234,7 @@ __global__ void __launch_bounds__(128) tc_tmap_kernel(const TcTmapParams p) {
   const bool use_a = a_side != swap;  // which operand's panel this map walks
   const long long off = use_a ? (lo ? pd.a_lo : pd.a_hi) : (lo ? pd.b_lo : pd.b_hi);
   const int rows = use_a ? d.M : d.N;
-  const int esz = (p.kind == kKindTF32) ? 4 : 2;
+  const int esz = (p.kind == kKindBF16) ? 2 : 4;
   const int box = a_side ? kTcBM : (p.pair ? tc2_cfg_bn(d.cfg) / 2 : tc_cfg_bn(d.cfg));
   const long long extent = (long long)rows * pd.kpad * esz;
   const CUtensorMap* tpl = p.templ + tmap_template_index(box, extent >= kTmapLargeExtent);

@@ -31,6 +31,8 @@ struct TcPlan {
   bool pair = false;   // CTA-pair kernel (tc2_kernel.cu)
   int clusters = 0;    // CTA pairs resident at once
   bool host_tmaps = false;  // encode every tensor map on the host (comparison path)
+  bool presplit = false;    // keep hi/lo pre-split operands even on CTA pairs
+  bool raw = false;         // 3xTF32 on pairs: raw FP32 operands split in the kernel
 };
 
 static inline long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
@@ -62,6 +64,7 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
   t->split = (p->mode == BGEMM_MODE_TF32) ? 0 : 1;
   t->nprod = t->split ? 3 : 1;
   t->host_tmaps = opt && opt->host_tensor_maps;
+  t->presplit = opt && opt->presplit_operands;
   p->tc = t;
   if (opt && opt->force_tile_config >= 0)
     t->pair = tc_cfg_pair(opt->force_tile_config);
@@ -71,7 +74,8 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
     return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1,
                      "CTA-pair tiles serve the split modes only");
   if (t->pair) {
-    t->clusters = tc2_max_clusters();
+    const bool raw_ok = p->mode == BGEMM_MODE_TF32X3 && !t->presplit;
+    t->clusters = raw_ok ? tc2s_max_clusters() : tc2_max_clusters();
     if (t->clusters < 1) {
       if (opt && opt->force_tile_config >= 0)
         return set_error(BGEMM_ERROR_NOT_SUPPORTED, 11, -1, "no CTA pair fits on this device");
@@ -105,9 +109,11 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
                        makespan(two, t->clusters) < makespan(one, single_slots));
     t->pair = pair;
     mp = pair ? two : one;
+    t->raw = t->pair && p->mode == BGEMM_MODE_TF32X3 && !t->presplit;
     return BGEMM_SUCCESS;
   }
   g_pair = t->pair;
+  t->raw = t->pair && p->mode == BGEMM_MODE_TF32X3 && !t->presplit;
   const int slots = t->pair ? t->clusters : single_slots;
   return choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, slots, opt, mp);
 }
@@ -141,13 +147,13 @@ static bool encode_panel(CUtensorMap* out, int kind, void* base, int K, int rows
                          int box_rows) {
   auto fn = encode_fn();
   if (!fn) return false;
-  const int esz = (kind == kKindTF32) ? 4 : 2;
+  const int esz = (kind == kKindBF16) ? 2 : 4;  // TF32 halves and raw FP32: 4 bytes
   cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)kpad * esz};
   cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(out, kind == kKindTF32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
-                                         : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+  CUresult r = fn(out, kind == kKindBF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                         : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
                   2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -157,7 +163,12 @@ static bool encode_panel(CUtensorMap* out, int kind, void* base, int K, int rows
 bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream) {
   TcPlan* t = p->tc;
   const int batch = p->batch;
-  const int esz = (t->kind == kKindTF32) ? 4 : 2;
+  if (t->raw) {
+    // 3xTF32 on CTA pairs: compact raw FP32 operands, split in the kernel
+    t->kind = kKindRaw;
+    t->split = 0;
+  }
+  const int esz = (t->kind == kKindBF16) ? 2 : 4;
   const int parts = t->split ? 2 : 1;
   const std::vector<MatDesc>& hd = p->host_descs;
 
@@ -336,8 +347,9 @@ bgemm_status_t tc_execute(bgemm_plan_s* p, float alpha, const float* const* dA,
   TcGemmParams gp{p->d_descs, p->d_items, p->n_items, p->d_counters, t->d_tmaps, alpha, beta,
                   dC, t->d_err, 2000000000ull};
   if (p->ev_start) cudaEventRecord(p->ev_start, stream);
-  e = t->pair ? tc2_gemm_launch(t->kind, gp, p->grid, stream)
-              : tc_gemm_launch(t->kind, t->split, gp, p->grid, stream);
+  e = t->raw    ? tc2s_gemm_launch(gp, p->grid, stream)
+      : t->pair ? tc2_gemm_launch(t->kind, gp, p->grid, stream)
+                : tc_gemm_launch(t->kind, t->split, gp, p->grid, stream);
   if (p->ev_stop) cudaEventRecord(p->ev_stop, stream);
   if (e != cudaSuccess) return cuda_error(e, "tcgen05 GEMM launch");
   return BGEMM_SUCCESS;

@@ -40,6 +40,32 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t a, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// Cluster-scope acquire, for barriers that receive arrivals from the peer CTA.
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Make this thread's generic-proxy writes to shared memory visible to the
+// async proxy (TMA, tcgen05.mma) before signalling the consumer.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// Round to nearest, ties to even, keeping 23 - drop explicit mantissa bits
+// (TF32: drop 13, BF16: drop 16); Inf and NaN pass through.
+__device__ __forceinline__ float round_keep(float x, int drop) {
+  uint32_t u = __float_as_uint(x);
+  if ((u & 0x7f800000u) == 0x7f800000u) return x;
+  const uint32_t half = (1u << (drop - 1)) - 1u;
+  u += half + ((u >> drop) & 1u);
+  u &= ~((1u << drop) - 1u);
+  return __uint_as_float(u);
+}
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1,
                                             uint32_t bar) {
   asm volatile(
@@ -146,6 +172,26 @@ __device__ __noinline__ bool wait_bounded(uint32_t bar, uint32_t parity, int* er
   const uint64_t t0 = gtimer();
   for (uint32_t i = 1;; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63u) == 0) {
+      if (abort && *abort) return false;
+      if (gtimer() - t0 > limit_ns) {
+        atomicOr(err, 1);
+        if (abort) *abort = 1;
+        return false;
+      }
+    }
+  }
+}
+
+// Bounded wait with cluster-scope acquire (barriers with arrivals from the
+// peer CTA or commits multicast by the leader).
+__device__ __noinline__ bool wait_bounded_cluster(uint32_t bar, uint32_t parity, int* err,
+                                                  volatile int* abort,
+                                                  unsigned long long limit_ns) {
+  if (mbar_try_wait_cluster(bar, parity)) return true;
+  const uint64_t t0 = gtimer();
+  for (uint32_t i = 1;; ++i) {
+    if (mbar_try_wait_cluster(bar, parity)) return true;
     if ((i & 63u) == 0) {
       if (abort && *abort) return false;
       if (gtimer() - t0 > limit_ns) {

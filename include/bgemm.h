@@ -92,7 +92,10 @@ typedef struct bgemm_plan_options {
   int disable_rebalance;    /* 1: skip the parallelism (wavefront) rebalance    */
   int host_tensor_maps;     /* 1: encode the TMA tensor maps on the host instead
                                of building them on the device (for comparison) */
-  int reserved[7];
+  int presplit_operands;    /* 1: TF32X3 on CTA pairs keeps hi/lo operands split by
+                               the pre-pass instead of splitting raw FP32 in the
+                               kernel (for comparison) */
+  int reserved[6];
 } bgemm_plan_options_t;
 
 /* --- one-shot entry (host size arrays, like CUDA/framework/gemm.cu:39-41) ---
