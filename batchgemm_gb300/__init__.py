@@ -61,7 +61,7 @@ class PlanInfo(ctypes.Structure):
 class PlanOptions(ctypes.Structure):
     _fields_ = [("force_tile_config", ctypes.c_int), ("max_ctas", ctypes.c_int),
                 ("disable_rebalance", ctypes.c_int), ("host_tensor_maps", ctypes.c_int),
-                ("presplit_operands", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+                ("split_in_kernel", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
 
 
 def build(**kw) -> str:
@@ -149,7 +149,7 @@ class Plan:
 
     def __init__(self, M, N, K, lda, ldb, ldc, mode="simt", stream=None,
                  force_tile_config: int = -1, max_ctas: int = 0, rebalance: bool = True,
-                 host_tensor_maps: bool = False, presplit_operands: bool = False):
+                 host_tensor_maps: bool = False, split_in_kernel: bool = False):
         self._h = ctypes.c_void_p()
         self.batch = len(M)
         opt = PlanOptions()
@@ -157,7 +157,7 @@ class Plan:
         opt.max_ctas = max_ctas
         opt.disable_rebalance = 0 if rebalance else 1
         opt.host_tensor_maps = 1 if host_tensor_maps else 0
-        opt.presplit_operands = 1 if presplit_operands else 0
+        opt.split_in_kernel = 1 if split_in_kernel else 0
         _check(lib().bgemm_plan_create_ex(ctypes.byref(self._h), _iarr(M), _iarr(N), _iarr(K),
                                           _iarr(lda), _iarr(ldb), _iarr(ldc), len(M),
                                           _mode(mode), _stream(stream), ctypes.byref(opt)))

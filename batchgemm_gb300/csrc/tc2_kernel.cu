@@ -199,7 +199,10 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
               }
               tc_fence_after();
               const uint32_t buf = tmem + acc.idx * 256u;
-              mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + 32u * s), idesc, 0u);
+              // small K: the split error dominates, so lo*lo is kept too
+              mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + kB + 32u * s),
+                             idesc, 0u);
+              mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
               mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + kB + 32u * s), idesc, 1u);
               mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
               mma_commit_pair(tfull(acc.idx));

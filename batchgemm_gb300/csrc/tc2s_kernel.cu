@@ -192,8 +192,11 @@ __global__ void __launch_bounds__(kThreadsS, 1) tc2s_gemm_kernel(const TcGemmPar
               }
               tc_fence_after();
               const uint32_t buf = tmem + acc.idx * 256u;
+              // small K: the split error dominates, so lo*lo is kept too
+              mma_pair<kKindTF32>(buf, sw128_desc(sa + kTile + 32u * s),
+                                  sw128_desc(sb + kTile + 32u * s), idesc, 0u);
               mma_pair<kKindTF32>(buf, sw128_desc(sa + kTile + 32u * s), sw128_desc(sb + 32u * s),
-                                  idesc, 0u);
+                                  idesc, 1u);
               mma_pair<kKindTF32>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + kTile + 32u * s),
                                   idesc, 1u);
               mma_pair<kKindTF32>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc,

@@ -404,7 +404,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
                 const uint32_t buf = tmem + acc.idx * 128u;
                 const uint64_t ah = sw128_desc(sa + 32u * s), al = sw128_desc(sa + kABytes + 32u * s);
                 const uint64_t bh = sw128_desc(sb + 32u * s), bl = sw128_desc(sb + kBBytes + 32u * s);
-                mma<KIND>(buf, al, bh, idesc, 0u);
+                // small K: the split error dominates, so lo*lo is kept too
+                mma<KIND>(buf, al, bl, idesc, 0u);
+                mma<KIND>(buf, al, bh, idesc, 1u);
                 mma<KIND>(buf, ah, bl, idesc, 1u);
                 mma<KIND>(buf, ah, bh, idesc, 1u);
                 mma_commit(tfull(acc.idx));

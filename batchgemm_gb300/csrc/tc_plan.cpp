@@ -31,7 +31,7 @@ struct TcPlan {
   bool pair = false;   // CTA-pair kernel (tc2_kernel.cu)
   int clusters = 0;    // CTA pairs resident at once
   bool host_tmaps = false;  // encode every tensor map on the host (comparison path)
-  bool presplit = false;    // keep hi/lo pre-split operands even on CTA pairs
+  bool split_in_kernel = false;  // 3xTF32 on pairs: split raw FP32 in shared memory
   bool raw = false;         // 3xTF32 on pairs: raw FP32 operands split in the kernel
 };
 
@@ -64,7 +64,7 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
   t->split = (p->mode == BGEMM_MODE_TF32) ? 0 : 1;
   t->nprod = t->split ? 3 : 1;
   t->host_tmaps = opt && opt->host_tensor_maps;
-  t->presplit = opt && opt->presplit_operands;
+  t->split_in_kernel = opt && opt->split_in_kernel;
   p->tc = t;
   if (opt && opt->force_tile_config >= 0)
     t->pair = tc_cfg_pair(opt->force_tile_config);
@@ -74,7 +74,7 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
     return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1,
                      "CTA-pair tiles serve the split modes only");
   if (t->pair) {
-    const bool raw_ok = p->mode == BGEMM_MODE_TF32X3 && !t->presplit;
+    const bool raw_ok = p->mode == BGEMM_MODE_TF32X3 && t->split_in_kernel;
     t->clusters = raw_ok ? tc2s_max_clusters() : tc2_max_clusters();
     if (t->clusters < 1) {
       if (opt && opt->force_tile_config >= 0)
@@ -109,11 +109,11 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
                        makespan(two, t->clusters) < makespan(one, single_slots));
     t->pair = pair;
     mp = pair ? two : one;
-    t->raw = t->pair && p->mode == BGEMM_MODE_TF32X3 && !t->presplit;
+    t->raw = t->pair && p->mode == BGEMM_MODE_TF32X3 && t->split_in_kernel;
     return BGEMM_SUCCESS;
   }
   g_pair = t->pair;
-  t->raw = t->pair && p->mode == BGEMM_MODE_TF32X3 && !t->presplit;
+  t->raw = t->pair && p->mode == BGEMM_MODE_TF32X3 && t->split_in_kernel;
   const int slots = t->pair ? t->clusters : single_slots;
   return choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, slots, opt, mp);
 }

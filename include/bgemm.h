@@ -92,9 +92,12 @@ typedef struct bgemm_plan_options {
   int disable_rebalance;    /* 1: skip the parallelism (wavefront) rebalance    */
   int host_tensor_maps;     /* 1: encode the TMA tensor maps on the host instead
                                of building them on the device (for comparison) */
-  int presplit_operands;    /* 1: TF32X3 on CTA pairs keeps hi/lo operands split by
-                               the pre-pass instead of splitting raw FP32 in the
-                               kernel (for comparison) */
+  int split_in_kernel;      /* 1: TF32X3 on CTA pairs loads raw FP32 operands (4 B
+                               per element) and splits them in shared memory
+                               instead of reading hi/lo pairs split by the
+                               pre-pass.  Fewer HBM/L2 bytes, but on GB300 the
+                               extra shared-memory traffic makes it slower, so
+                               it is off by default (kept for comparison). */
   int reserved[6];
 } bgemm_plan_options_t;
 

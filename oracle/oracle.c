@@ -140,7 +140,8 @@ void bgo_split(int mode, const float* x, size_t n, float* hi, float* lo) {
 
 /* Exact (FP64) value of the products a tensor-core mode forms:
  *   TF32   : hi(a)*hi(b)
- *   TF32X3 : hi(a)*hi(b) + hi(a)*lo(b) + lo(a)*hi(b)
+ *   TF32X3 : hi(a)*hi(b) + hi(a)*lo(b) + lo(a)*hi(b), plus lo(a)*lo(b) when
+ *            K <= 64 (short inner products, where the split error dominates)
  *   BF16X3 : the same with bfloat16 halves.
  * Every product of two rounded halves is exact in FP64 and K <= 2^20 keeps
  * the FP64 sum far below FP32 resolution, so the only gap left between this
@@ -166,7 +167,10 @@ void bgo_sgemm_split_f64(int mode, int M, int N, int K, double alpha,
       const float* aL = al + (size_t)k * M;
       for (int m = 0; m < M; ++m) {
         double p = (double)aH[m] * bhk;
-        if (mode != BGO_MODE_TF32) p += (double)aH[m] * blk + (double)aL[m] * bhk;
+        if (mode != BGO_MODE_TF32) {
+          p += (double)aH[m] * blk + (double)aL[m] * bhk;
+          if (K <= 64) p += (double)aL[m] * blk;
+        }
         acc[m] += p;
       }
     }
