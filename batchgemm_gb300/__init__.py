@@ -58,10 +58,48 @@ class PlanInfo(ctypes.Structure):
         }
 
 
+class PlanRequirements(ctypes.Structure):
+    """bgemm_plan_requirements_t: device sizes of a batch inside a plan."""
+    _fields_ = [("batch", ctypes.c_int), ("tiles", ctypes.c_int), ("pack_jobs", ctypes.c_int),
+                ("kernel_family", ctypes.c_int), ("workspace_bytes", ctypes.c_size_t),
+                ("reserved", ctypes.c_int * 4)]
+
+    def as_dict(self):
+        return {"batch": self.batch, "tiles": self.tiles, "pack_jobs": self.pack_jobs,
+                "kernel_family": self.kernel_family, "workspace_bytes": self.workspace_bytes}
+
+    @classmethod
+    def from_dict(cls, d):
+        r = cls()
+        for k in ("batch", "tiles", "pack_jobs", "kernel_family", "workspace_bytes"):
+            setattr(r, k, int(d.get(k, 0)))
+        return r
+
+
+KERNEL_FAMILIES = {"auto": 0, "single": 1, "pair": 2}
+
+
 class PlanOptions(ctypes.Structure):
     _fields_ = [("force_tile_config", ctypes.c_int), ("max_ctas", ctypes.c_int),
                 ("disable_rebalance", ctypes.c_int), ("host_tensor_maps", ctypes.c_int),
-                ("split_in_kernel", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+                ("split_in_kernel", ctypes.c_int), ("kernel_family", ctypes.c_int),
+                ("reserved", ctypes.c_int * 5), ("capacity", PlanRequirements)]
+
+
+def _options(force_tile_config=-1, max_ctas=0, rebalance=True, host_tensor_maps=False,
+             split_in_kernel=False, kernel_family="auto", capacity=None) -> PlanOptions:
+    opt = PlanOptions()
+    opt.force_tile_config = force_tile_config
+    opt.max_ctas = max_ctas
+    opt.disable_rebalance = 0 if rebalance else 1
+    opt.host_tensor_maps = 1 if host_tensor_maps else 0
+    opt.split_in_kernel = 1 if split_in_kernel else 0
+    opt.kernel_family = (KERNEL_FAMILIES[kernel_family] if isinstance(kernel_family, str)
+                         else int(kernel_family))
+    if capacity is not None:
+        opt.capacity = (capacity if isinstance(capacity, PlanRequirements)
+                        else PlanRequirements.from_dict(capacity))
+    return opt
 
 
 def build(**kw) -> str:
@@ -87,6 +125,11 @@ def lib() -> ctypes.CDLL:
                                        ctypes.POINTER(PlanOptions)]
     L.bgemm_plan_execute.argtypes = [vp, f, vp, vp, f, vp, vp]
     L.bgemm_plan_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
+    L.bgemm_plan_requirements.argtypes = [ip, ip, ip, ip, ip, ip, i, i,
+                                          ctypes.POINTER(PlanOptions),
+                                          ctypes.POINTER(PlanRequirements)]
+    L.bgemm_plan_update.argtypes = [vp, ip, ip, ip, ip, ip, ip, i, vp]
+    L.bgemm_plan_capacity.argtypes = [vp, ctypes.POINTER(PlanRequirements)]
     L.bgemm_plan_check_device.argtypes = [vp, vp]
     L.bgemm_plan_set_kernel_events.argtypes = [vp, vp, vp]
     L.bgemm_plan_destroy.argtypes = [vp]
@@ -104,7 +147,8 @@ def lib() -> ctypes.CDLL:
                  "bgemm_plan_execute", "bgemm_plan_info", "bgemm_plan_check_device",
                  "bgemm_plan_destroy", "bgemm_framework_gemm", "bgemm_framework_check_device",
                  "bgemm_framework_gemm_noalloc", "bgemm_device_info",
-                 "bgemm_plan_set_kernel_events"):
+                 "bgemm_plan_set_kernel_events", "bgemm_plan_requirements",
+                 "bgemm_plan_update", "bgemm_plan_capacity"):
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -120,8 +164,15 @@ def _check(status: int) -> None:
 
 
 def _iarr(v: Sequence[int]):
+    if isinstance(v, ctypes.Array):  # already converted (hot loops convert once)
+        return v
     n = len(v)
     return (ctypes.c_int * max(n, 1))(*[int(x) for x in v])
+
+
+def int_array(v: Sequence[int]):
+    """A ctypes int array for the size arguments (convert once, reuse in loops)."""
+    return _iarr(v)
 
 
 def _mode(mode) -> int:
@@ -144,20 +195,37 @@ def sgemm_vbatched(M, N, K, alpha, dA, lda, dB, ldb, beta, dC, ldc, mode="simt",
                                       len(M), _mode(mode), _stream(stream)))
 
 
+def plan_requirements(M, N, K, lda, ldb, ldc, mode="simt", **options) -> dict:
+    """bgemm_plan_requirements: the device sizes a batch needs in a plan made
+    with these options (host-only planning, nothing allocated)."""
+    opt = _options(**options)
+    out = PlanRequirements()
+    _check(lib().bgemm_plan_requirements(_iarr(M), _iarr(N), _iarr(K), _iarr(lda), _iarr(ldb),
+                                         _iarr(ldc), len(M), _mode(mode), ctypes.byref(opt),
+                                         ctypes.byref(out)))
+    return out.as_dict()
+
+
+def max_requirements(reqs) -> dict:
+    """Element-wise maximum of requirement dicts (a capacity for all of them)."""
+    out = {"batch": 0, "tiles": 0, "pack_jobs": 0, "kernel_family": 0, "workspace_bytes": 0}
+    for r in reqs:
+        for k in out:
+            out[k] = max(out[k], int(r[k]))
+    return out
+
+
 class Plan:
-    """bgemm_plan_create / execute / destroy."""
+    """bgemm_plan_create / execute / update / destroy."""
 
     def __init__(self, M, N, K, lda, ldb, ldc, mode="simt", stream=None,
                  force_tile_config: int = -1, max_ctas: int = 0, rebalance: bool = True,
-                 host_tensor_maps: bool = False, split_in_kernel: bool = False):
+                 host_tensor_maps: bool = False, split_in_kernel: bool = False,
+                 kernel_family="auto", capacity=None):
         self._h = ctypes.c_void_p()
         self.batch = len(M)
-        opt = PlanOptions()
-        opt.force_tile_config = force_tile_config
-        opt.max_ctas = max_ctas
-        opt.disable_rebalance = 0 if rebalance else 1
-        opt.host_tensor_maps = 1 if host_tensor_maps else 0
-        opt.split_in_kernel = 1 if split_in_kernel else 0
+        opt = _options(force_tile_config, max_ctas, rebalance, host_tensor_maps,
+                       split_in_kernel, kernel_family, capacity)
         _check(lib().bgemm_plan_create_ex(ctypes.byref(self._h), _iarr(M), _iarr(N), _iarr(K),
                                           _iarr(lda), _iarr(ldb), _iarr(ldc), len(M),
                                           _mode(mode), _stream(stream), ctypes.byref(opt)))
@@ -165,6 +233,18 @@ class Plan:
     def execute(self, alpha, dA, dB, beta, dC, stream=None) -> None:
         _check(lib().bgemm_plan_execute(self._h, float(alpha), dA, dB, float(beta), dC,
                                         _stream(stream)))
+
+    def update(self, M, N, K, lda, ldb, ldc, stream=None) -> None:
+        """bgemm_plan_update: re-plan a new batch into this plan's buffers."""
+        n = len(M)
+        _check(lib().bgemm_plan_update(self._h, _iarr(M), _iarr(N), _iarr(K), _iarr(lda),
+                                       _iarr(ldb), _iarr(ldc), n, _stream(stream)))
+        self.batch = n
+
+    def capacity(self) -> dict:
+        out = PlanRequirements()
+        _check(lib().bgemm_plan_capacity(self._h, ctypes.byref(out)))
+        return out.as_dict()
 
     def info(self) -> dict:
         inf = PlanInfo()

@@ -270,10 +270,162 @@ int debug_simt_queue(const int* M, const int* N, const int* K, int batch, int sl
 
 static void free_plan_memory(bgemm_plan_s* p) {
   if (p->d_mem) cudaFree(p->d_mem);
-  if (p->h_pinned) cudaFreeHost(p->h_pinned);
+  for (int s = 0; s < 2; ++s) {
+    if (p->h_stage[s]) cudaFreeHost(p->h_stage[s]);
+    if (p->ev_stage[s]) cudaEventDestroy(p->ev_stage[s]);
+    p->h_stage[s] = nullptr;
+    p->ev_stage[s] = nullptr;
+  }
   if (p->tc) tc_plan_release(p);
   p->d_mem = nullptr;
-  p->h_pinned = nullptr;
+}
+
+static bgemm_plan_options_t default_options() {
+  bgemm_plan_options_t o{};
+  o.force_tile_config = -1;
+  return o;
+}
+
+// Host planning of one batch: tile choice, largest-first queue, descriptors
+// and (tensor-core modes) the pre-pass layout.  Touches no device memory.
+static bgemm_status_t plan_batch(bgemm_plan_s* p, const int* M, const int* N, const int* K,
+                                 const int* lda, const int* ldb, const int* ldc, int batch,
+                                 bool first, BatchPlan& bp) {
+  std::vector<MatPlan> mp;
+  bgemm_status_t st;
+  if (p->mode == BGEMM_MODE_SIMT_FP32)
+    st = choose_simt(M, N, K, batch, p->facts.num_sms * p->facts.simt_ctas_per_sm, &p->opt, mp);
+  else
+    st = tc_choose(p, M, N, K, batch, first, mp);
+  if (st != BGEMM_SUCCESS) return st;
+  std::vector<int> order;
+  const long long n_items = order_matrices(mp, order);
+  if (n_items > (1LL << 31) - 1024)
+    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 0, -1, "batch has %lld tiles", n_items);
+  bp.batch = batch;
+  bp.descs.resize(batch);
+  bp.items.resize((size_t)n_items);
+  std::memset(bp.hist, 0, sizeof(bp.hist));
+  bp.flops = bp.bytes = 0;
+  for (int i = 0; i < batch; ++i) {
+    bp.descs[i] = MatDesc{M[i], N[i], K[i], lda[i], ldb[i], ldc[i], mp[i].cfg < 0 ? 0 : mp[i].cfg, 0};
+    bp.flops += 2.0 * M[i] * (double)N[i] * K[i];
+    bp.bytes += 4.0 * ((double)M[i] * K[i] + (double)K[i] * N[i] + (double)M[i] * N[i]);
+    if (mp[i].cfg >= 0 && mp[i].cfg < 16) bp.hist[mp[i].cfg]++;
+  }
+  expand_items(p->mode, p, M, N, mp, order, bp.descs.data(), bp.items.data());
+  bp.req = bgemm_plan_requirements_t{};
+  bp.req.batch = batch;
+  bp.req.tiles = (int)n_items;
+  if (p->mode != BGEMM_MODE_SIMT_FP32) tc_layout(p, bp.descs, &bp.req);
+  return BGEMM_SUCCESS;
+}
+
+// Device buffers for the plan's capacity, pinned staging, launch shapes.
+static bgemm_status_t plan_alloc(bgemm_plan_s* p) {
+  p->off_descs = kHdrBytes;
+  p->off_items = p->off_descs + ((sizeof(MatDesc) * (size_t)p->cap.batch + 255) & ~size_t(255));
+  p->mem_bytes = p->off_items + ((sizeof(TileItem) * (size_t)p->cap.tiles + 255) & ~size_t(255));
+  cudaError_t e = cudaMalloc(&p->d_mem, p->mem_bytes);
+  if (e != cudaSuccess)
+    return set_error(BGEMM_ERROR_ALLOC, 0, -1, "device plan memory of %zu bytes: %s", p->mem_bytes,
+                     cudaGetErrorString(e));
+  for (int s = 0; s < 2; ++s) {
+    e = cudaMallocHost(&p->h_stage[s], p->mem_bytes);
+    if (e != cudaSuccess)
+      return set_error(BGEMM_ERROR_ALLOC, 0, -1, "pinned staging of %zu bytes: %s", p->mem_bytes,
+                       cudaGetErrorString(e));
+    e = cudaEventCreateWithFlags(&p->ev_stage[s], cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_error(e, "staging event");
+  }
+  char* d = static_cast<char*>(p->d_mem);
+  p->d_counters = reinterpret_cast<int*>(d);
+  p->d_descs = reinterpret_cast<MatDesc*>(d + p->off_descs);
+  p->d_items = reinterpret_cast<TileItem*>(d + p->off_items);
+  const DeviceFacts& df = p->facts;
+  const int ctas_per_sm =
+      (p->mode == BGEMM_MODE_SIMT_FP32) ? df.simt_ctas_per_sm : df.tc_ctas_per_sm;
+  long long grid = (long long)df.num_sms * ctas_per_sm;
+  if (p->opt.max_ctas > 0) grid = std::min<long long>(grid, p->opt.max_ctas);
+  grid = std::min<long long>(grid, std::max(p->cap.tiles, 1));
+  p->grid = (int)grid;
+  p->info.grid = p->grid;
+  p->info.device_bytes = p->mem_bytes;
+  p->info.kernels_per_execute = (p->mode == BGEMM_MODE_SIMT_FP32) ? 1 : 2;
+  if (p->mode != BGEMM_MODE_SIMT_FP32) return tc_alloc(p);
+  return BGEMM_SUCCESS;
+}
+
+// Stages a planned batch in the next pinned buffer and uploads it on
+// `stream`.  The buffer's previous upload (two commits ago) must have been
+// consumed before it is rewritten.
+static bgemm_status_t plan_commit(bgemm_plan_s* p, BatchPlan& bp, bool first,
+                                  cudaStream_t stream) {
+  const int s = p->stage;
+  cudaError_t e = cudaSuccess;
+  if (p->stage_used[s]) {
+    e = cudaEventSynchronize(p->ev_stage[s]);
+    if (e != cudaSuccess) return cuda_error(e, "waiting for the staging buffer");
+  }
+  char* h = static_cast<char*>(p->h_stage[s]);
+  char* d = static_cast<char*>(p->d_mem);
+  std::memset(h, 0, kHdrBytes);
+  int* hdr = reinterpret_cast<int*>(h);
+  hdr[kHdrItems] = bp.req.tiles;
+  hdr[kHdrJobs] = bp.req.pack_jobs;
+  if (bp.batch) std::memcpy(h + p->off_descs, bp.descs.data(), sizeof(MatDesc) * bp.descs.size());
+  if (!bp.items.empty())
+    std::memcpy(h + p->off_items, bp.items.data(), sizeof(TileItem) * bp.items.size());
+  auto copy = [&](size_t off, size_t bytes) {
+    return bytes ? cudaMemcpyAsync(d + off, h + off, bytes, cudaMemcpyHostToDevice, stream)
+                 : cudaSuccess;
+  };
+  e = copy(0, kHdrBytes);
+  if (e == cudaSuccess) e = copy(p->off_descs, sizeof(MatDesc) * bp.descs.size());
+  if (e == cudaSuccess) e = copy(p->off_items, sizeof(TileItem) * bp.items.size());
+  if (e != cudaSuccess) return cuda_error(e, "descriptor upload");
+  p->batch = bp.batch;
+  p->n_items = bp.req.tiles;
+  p->host_descs.swap(bp.descs);
+  if (p->mode != BGEMM_MODE_SIMT_FP32) {
+    bgemm_status_t st = tc_commit(p, s, p->batch, first, stream);
+    if (st != BGEMM_SUCCESS) return st;
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(stream, &cs);
+  if (cs != cudaStreamCaptureStatusNone) {
+    // created inside a capture: the graph's copies read this staging buffer
+    // whenever it runs, so it may never be rewritten (updates are refused)
+    p->staged_in_capture = true;
+  } else {
+    e = cudaEventRecord(p->ev_stage[s], stream);
+    if (e != cudaSuccess) return cuda_error(e, "staging event record");
+    p->stage_used[s] = true;
+  }
+  p->stage ^= 1;
+  p->info.batch = p->batch;
+  p->info.num_tiles = p->n_items;
+  std::memcpy(p->info.tile_config_hist, bp.hist, sizeof(bp.hist));
+  p->info.useful_flops = bp.flops;
+  p->info.min_bytes = bp.bytes;
+  return BGEMM_SUCCESS;
+}
+
+static bgemm_status_t check_capacity_option(const bgemm_plan_requirements_t& c) {
+  if (c.batch < 0 || c.tiles < 0 || c.pack_jobs < 0)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1, "negative capacity");
+  return BGEMM_SUCCESS;
+}
+
+static bgemm_status_t stream_not_capturing(cudaStream_t stream, int arg) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(stream, &cs);
+  if (e != cudaSuccess) return cuda_error(e, "cudaStreamIsCapturing");
+  if (cs != cudaStreamCaptureStatusNone)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, arg, -1,
+                     "the stream is capturing: re-planning writes host staging buffers "
+                     "that a captured copy would read later");
+  return BGEMM_SUCCESS;
 }
 
 bgemm_status_t plan_create(bgemm_plan_t* out, const int* M, const int* N, const int* K,
@@ -283,118 +435,105 @@ bgemm_status_t plan_create(bgemm_plan_t* out, const int* M, const int* N, const 
   *out = nullptr;
   bgemm_status_t st = check_args(M, N, K, lda, ldb, ldc, batch, mode, 2, 3, 4, 5, 6, 7, 8, 9);
   if (st != BGEMM_SUCCESS) return st;
+  if (opt && (st = check_capacity_option(opt->capacity)) != BGEMM_SUCCESS) return st;
   DeviceFacts df;
   st = device_facts(&df);
   if (st != BGEMM_SUCCESS) return st;
 
   auto* p = new bgemm_plan_s();
-  p->batch = batch;
   p->mode = mode;
   p->facts = df;
-  p->info.batch = batch;
+  p->opt = opt ? *opt : default_options();
   p->info.mode = mode;
-
-  std::vector<MatPlan> mp;
-  if (mode == BGEMM_MODE_SIMT_FP32) {
-    const int slots = df.num_sms * df.simt_ctas_per_sm;
-    st = choose_simt(M, N, K, batch, slots, opt, mp);
-  } else {
-    st = tc_choose(p, M, N, K, batch, opt, mp);
+  BatchPlan bp;
+  if (mode != BGEMM_MODE_SIMT_FP32) st = tc_init(p, &p->opt);
+  if (st == BGEMM_SUCCESS) st = plan_batch(p, M, N, K, lda, ldb, ldc, batch, true, bp);
+  if (st == BGEMM_SUCCESS) {
+    const bgemm_plan_requirements_t& c = p->opt.capacity;
+    p->cap = bp.req;
+    p->cap.batch = std::max(p->cap.batch, c.batch);
+    p->cap.tiles = std::max(p->cap.tiles, c.tiles);
+    p->cap.pack_jobs = std::max(p->cap.pack_jobs, c.pack_jobs);
+    p->cap.workspace_bytes = std::max(p->cap.workspace_bytes, c.workspace_bytes);
+    st = plan_alloc(p);
   }
+  if (st == BGEMM_SUCCESS) st = plan_commit(p, bp, true, stream);
   if (st != BGEMM_SUCCESS) {
     free_plan_memory(p);
     delete p;
     return st;
   }
-
-  std::vector<int> order;
-  const long long n_items = order_matrices(mp, order);
-  if (n_items > (1LL << 31) - 1024) {
-    delete p;
-    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 0, -1, "batch has %lld tiles", n_items);
-  }
-  p->n_items = (int)n_items;
-
-  // host staging layout: [counters 256 B][descs][items][mode extras]
-  const size_t off_desc = 256;
-  const size_t off_items = off_desc + ((sizeof(MatDesc) * (size_t)batch + 255) & ~size_t(255));
-  const size_t end_items = off_items + ((sizeof(TileItem) * (size_t)n_items + 255) & ~size_t(255));
-  size_t total = end_items;
-  size_t tc_extra = 0;
-  if (mode != BGEMM_MODE_SIMT_FP32) tc_extra = tc_extra_bytes(p, batch);
-  total += tc_extra;
-
-  cudaError_t e = cudaMallocHost(&p->h_pinned, end_items);
-  if (e != cudaSuccess) {
-    delete p;
-    return set_error(BGEMM_ERROR_ALLOC, 0, -1, "pinned staging of %zu bytes: %s", end_items,
-                     cudaGetErrorString(e));
-  }
-  e = cudaMalloc(&p->d_mem, total);
-  if (e != cudaSuccess) {
-    free_plan_memory(p);
-    delete p;
-    return set_error(BGEMM_ERROR_ALLOC, 0, -1, "device plan memory of %zu bytes: %s", total,
-                     cudaGetErrorString(e));
-  }
-  char* h = static_cast<char*>(p->h_pinned);
-  std::memset(h, 0, 256);
-  auto* hd = reinterpret_cast<MatDesc*>(h + off_desc);
-  auto* hi = reinterpret_cast<TileItem*>(h + off_items);
-  double flops = 0, bytes = 0;
-  for (int i = 0; i < batch; ++i) {
-    hd[i] = MatDesc{M[i], N[i], K[i], lda[i], ldb[i], ldc[i], mp[i].cfg < 0 ? 0 : mp[i].cfg, 0};
-    flops += 2.0 * M[i] * (double)N[i] * K[i];
-    bytes += 4.0 * ((double)M[i] * K[i] + (double)K[i] * N[i] + (double)M[i] * N[i]);
-    if (mp[i].cfg >= 0 && mp[i].cfg < 16) p->info.tile_config_hist[mp[i].cfg]++;
-  }
-  expand_items(mode, p, M, N, mp, order, hd, hi);
-  p->host_descs.assign(hd, hd + batch);
-  p->info.kernels_per_execute = (mode == BGEMM_MODE_SIMT_FP32) ? 1 : 2;
-  p->d_counters = reinterpret_cast<int*>(static_cast<char*>(p->d_mem));
-  p->d_descs = reinterpret_cast<MatDesc*>(static_cast<char*>(p->d_mem) + off_desc);
-  p->d_items = reinterpret_cast<TileItem*>(static_cast<char*>(p->d_mem) + off_items);
-  p->d_extra = static_cast<char*>(p->d_mem) + end_items;
-
-  e = cudaMemcpyAsync(p->d_mem, p->h_pinned, end_items, cudaMemcpyHostToDevice, stream);
-  if (e != cudaSuccess) {
-    free_plan_memory(p);
-    delete p;
-    return cuda_error(e, "descriptor upload");
-  }
-  const int ctas_per_sm = (mode == BGEMM_MODE_SIMT_FP32) ? df.simt_ctas_per_sm : df.tc_ctas_per_sm;
-  long long grid = (long long)df.num_sms * ctas_per_sm;
-  if (opt && opt->max_ctas > 0) grid = std::min<long long>(grid, opt->max_ctas);
-  grid = std::min<long long>(grid, std::max<long long>(n_items, 1));
-  p->grid = (int)grid;
-
-  p->info.num_tiles = p->n_items;
-  p->info.grid = p->grid;
-  p->info.useful_flops = flops;
-  p->info.min_bytes = bytes;
-  p->info.device_bytes = total;
-  if (mode != BGEMM_MODE_SIMT_FP32) {
-    st = tc_plan_finish(p, stream);
-    if (st != BGEMM_SUCCESS) {
-      free_plan_memory(p);
-      delete p;
-      return st;
-    }
-  }
   *out = p;
   return BGEMM_SUCCESS;
+}
+
+bgemm_status_t plan_update(bgemm_plan_t p, const int* M, const int* N, const int* K,
+                           const int* lda, const int* ldb, const int* ldc, int batch,
+                           cudaStream_t stream) {
+  if (!p) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
+  bgemm_status_t st =
+      check_args(M, N, K, lda, ldb, ldc, batch, p->mode, 2, 3, 4, 5, 6, 7, 8, 8);
+  if (st != BGEMM_SUCCESS) return st;
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != p->facts.device)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan belongs to device %d, current is %d",
+                     p->facts.device, dev);
+  if ((st = stream_not_capturing(stream, 9)) != BGEMM_SUCCESS) return st;
+  if (p->staged_in_capture)
+    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 1, -1,
+                     "the plan was created during a stream capture; the captured upload reads "
+                     "its staging, so it cannot be updated");
+  if (batch > p->cap.batch)
+    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 8, -1, "batch %d exceeds the plan's capacity %d",
+                     batch, p->cap.batch);
+  BatchPlan bp;
+  st = plan_batch(p, M, N, K, lda, ldb, ldc, batch, false, bp);
+  if (st != BGEMM_SUCCESS) return st;
+  const bgemm_plan_requirements_t& r = bp.req;
+  if (r.tiles > p->cap.tiles || r.pack_jobs > p->cap.pack_jobs ||
+      r.workspace_bytes > p->cap.workspace_bytes)
+    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 0, -1,
+                     "batch needs %d tiles, %d pack jobs, %zu workspace bytes; the plan holds "
+                     "%d, %d, %zu",
+                     r.tiles, r.pack_jobs, r.workspace_bytes, p->cap.tiles, p->cap.pack_jobs,
+                     p->cap.workspace_bytes);
+  return plan_commit(p, bp, false, stream);
+}
+
+bgemm_status_t plan_requirements(const int* M, const int* N, const int* K, const int* lda,
+                                 const int* ldb, const int* ldc, int batch, int mode,
+                                 const bgemm_plan_options_t* opt,
+                                 bgemm_plan_requirements_t* out) {
+  bgemm_status_t st = check_args(M, N, K, lda, ldb, ldc, batch, mode, 1, 2, 3, 4, 5, 6, 7, 8);
+  if (st != BGEMM_SUCCESS) return st;
+  if (!out) return set_error(BGEMM_ERROR_INVALID_VALUE, 10, -1, "out is NULL");
+  DeviceFacts df;
+  st = device_facts(&df);
+  if (st != BGEMM_SUCCESS) return st;
+  bgemm_plan_s p;
+  p.mode = mode;
+  p.facts = df;
+  p.opt = opt ? *opt : default_options();
+  BatchPlan bp;
+  if (mode != BGEMM_MODE_SIMT_FP32) st = tc_init(&p, &p.opt);
+  if (st == BGEMM_SUCCESS) st = plan_batch(&p, M, N, K, lda, ldb, ldc, batch, true, bp);
+  if (p.tc) tc_plan_release(&p);
+  if (st == BGEMM_SUCCESS) *out = bp.req;
+  return st;
 }
 
 bgemm_status_t plan_execute(bgemm_plan_t p, float alpha, const float* const* dA,
                             const float* const* dB, float beta, float* const* dC,
                             cudaStream_t stream) {
   if (!p) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
-  if (p->n_items == 0) return BGEMM_SUCCESS;
+  if (p->cap.tiles == 0) return BGEMM_SUCCESS;
   if (!dA) return set_error(BGEMM_ERROR_INVALID_VALUE, 3, -1, "dA is NULL");
   if (!dB) return set_error(BGEMM_ERROR_INVALID_VALUE, 4, -1, "dB is NULL");
   if (!dC) return set_error(BGEMM_ERROR_INVALID_VALUE, 6, -1, "dC is NULL");
   if (p->mode == BGEMM_MODE_SIMT_FP32) {
-    SimtParams sp{p->d_descs, p->d_items, p->n_items, nullptr, p->d_counters, alpha, beta, dA, dB, dC};
+    SimtParams sp{p->d_descs, p->d_items,  p->n_items, p->d_counters + kHdrItems,
+                  p->d_counters, alpha,    beta,       dA, dB, dC};
     if (p->ev_start) cudaEventRecord(p->ev_start, stream);
     cudaError_t e = simt_launch(sp, p->grid, stream);
     if (p->ev_stop) cudaEventRecord(p->ev_stop, stream);
@@ -541,6 +680,35 @@ bgemm_status_t bgemm_plan_info(bgemm_plan_t plan, bgemm_plan_info_t* info) {
   if (!plan) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
   if (!info) return set_error(BGEMM_ERROR_INVALID_VALUE, 2, -1, "info is NULL");
   *info = plan->info;
+  return BGEMM_SUCCESS;
+}
+
+bgemm_status_t bgemm_plan_requirements(const int* M, const int* N, const int* K,
+                                       const int* lda, const int* ldb, const int* ldc, int batch,
+                                       bgemm_mode_t mode, const bgemm_plan_options_t* options,
+                                       bgemm_plan_requirements_t* out) {
+  clear_error();
+  if (options && options->force_tile_config >= 0) {
+    const int ncfg = (mode == BGEMM_MODE_SIMT_FP32) ? kSimtNumCfgs : kTcNumCfgs;
+    if (options->force_tile_config >= ncfg)
+      return set_error(BGEMM_ERROR_INVALID_VALUE, 9, -1, "force_tile_config %d >= %d",
+                       options->force_tile_config, ncfg);
+  }
+  return plan_requirements(M, N, K, lda, ldb, ldc, batch, (int)mode, options, out);
+}
+
+bgemm_status_t bgemm_plan_update(bgemm_plan_t plan, const int* M, const int* N, const int* K,
+                                 const int* lda, const int* ldb, const int* ldc, int batch,
+                                 bgemm_stream_t stream) {
+  clear_error();
+  return plan_update(plan, M, N, K, lda, ldb, ldc, batch, stream);
+}
+
+bgemm_status_t bgemm_plan_capacity(bgemm_plan_t plan, bgemm_plan_requirements_t* out) {
+  clear_error();
+  if (!plan) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
+  if (!out) return set_error(BGEMM_ERROR_INVALID_VALUE, 2, -1, "out is NULL");
+  *out = plan->cap;
   return BGEMM_SUCCESS;
 }
 

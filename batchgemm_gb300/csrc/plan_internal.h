@@ -29,6 +29,26 @@ constexpr int kTcSwapFlag = 1 << 30;
 // ids 0..7: one-SM tiles; ids 8..15: CTA-pair tiles (split modes)
 constexpr int kTcNumCfgs = 16;
 
+// The plan's device header (256 bytes, ints): [0] queue head and [1] CTAs
+// finished (reset by the kernels themselves), [kHdrItems] work items of the
+// current batch, [kHdrJobs] pre-pass jobs of the current batch.  Kernels read
+// the counts from here, so a captured launch serves every batch an update
+// uploads.
+constexpr int kHdrItems = 16;
+constexpr int kHdrJobs = 17;
+constexpr size_t kHdrBytes = 256;
+
+// Host result of planning one batch, before anything is written to the
+// plan's buffers (an update that does not fit leaves the plan untouched).
+struct BatchPlan {
+  int batch = 0;
+  std::vector<MatDesc> descs;
+  std::vector<TileItem> items;
+  int hist[16] = {};
+  double flops = 0, bytes = 0;
+  bgemm_plan_requirements_t req{};
+};
+
 }  // namespace bgemm
 
 struct bgemm_plan_s {
@@ -37,12 +57,18 @@ struct bgemm_plan_s {
   int n_items = 0;
   int grid = 0;
   bgemm::DeviceFacts facts{};
-  void* d_mem = nullptr;     // counters | descs | items | mode extras
-  void* h_pinned = nullptr;  // staging of counters | descs | items
-  int* d_counters = nullptr;
+  bgemm_plan_options_t opt{};      // options of creation, reused by updates
+  bgemm_plan_requirements_t cap{}; // capacity of the device buffers
+  void* d_mem = nullptr;           // header | descs[cap] | items[cap]
+  void* h_stage[2] = {nullptr, nullptr};  // double-buffered pinned staging, same layout
+  cudaEvent_t ev_stage[2] = {nullptr, nullptr};  // upload from h_stage[i] consumed
+  bool stage_used[2] = {false, false};
+  int stage = 0;                   // staging buffer of the next upload
+  bool staged_in_capture = false;  // created during a stream capture (no updates)
+  size_t off_descs = 0, off_items = 0, mem_bytes = 0;
+  int* d_counters = nullptr;       // the device header
   bgemm::MatDesc* d_descs = nullptr;
   bgemm::TileItem* d_items = nullptr;
-  char* d_extra = nullptr;
   bgemm::TcPlan* tc = nullptr;
   std::vector<bgemm::MatDesc> host_descs;
   bgemm_plan_info_t info{};
@@ -66,11 +92,21 @@ bgemm_status_t choose_tiles(int ncfg, TileEval eval, const int* M, const int* N,
                             std::vector<MatPlan>& mp);
 
 // tensor-core hooks (tc_plan.cpp)
+// tc_init: mode facts and option checks, once per plan.
+bgemm_status_t tc_init(bgemm_plan_s* p, const bgemm_plan_options_t* opt);
+// tc_choose: tile configurations of a batch; the first call of a plan also
+// fixes its kernel family (one-SM or CTA pair), later calls keep it.
 bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int* K, int batch,
-                         const bgemm_plan_options_t* opt, std::vector<MatPlan>& mp);
+                         bool first, std::vector<MatPlan>& mp);
 void tc_tile_dims(bgemm_plan_s* p, int i, int M, int N, int cfg, int* bm, int* bn, MatDesc* d);
-size_t tc_extra_bytes(bgemm_plan_s* p, int batch);
-bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream);
+// tc_layout: split-operand workspace offsets and pre-pass jobs of a planned
+// batch (kept in the TcPlan until tc_commit); fills the requirement fields.
+void tc_layout(bgemm_plan_s* p, const std::vector<MatDesc>& hd, bgemm_plan_requirements_t* req);
+// tc_alloc: device/pinned buffers for the plan's capacity, launch shapes.
+bgemm_status_t tc_alloc(bgemm_plan_s* p);
+// tc_commit: stage and upload the laid-out batch through staging buffer
+// `stage`, build its tensor maps (first: also templates and error word).
+bgemm_status_t tc_commit(bgemm_plan_s* p, int stage, int batch, bool first, cudaStream_t stream);
 bgemm_status_t tc_execute(bgemm_plan_s* p, float alpha, const float* const* dA,
                           const float* const* dB, float beta, float* const* dC,
                           cudaStream_t stream);

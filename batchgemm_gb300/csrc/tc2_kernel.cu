@@ -28,6 +28,7 @@
 // All waits are bounded as in tc_kernel.cu.
 #include <stdint.h>
 
+#include "tc_epilogue.h"
 #include "tc_ptx.h"
 
 namespace bgemm {
@@ -79,6 +80,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
+  const int n_items = p.n_items_dev ? *p.n_items_dev : p.n_items;
   const uint32_t rank = cluster_ctarank();
   const bool leader = rank == 0;
   const int cl = blockIdx.x >> 1;
@@ -119,7 +121,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       int last_mat = -1;
       for (int t = 0; ok; ++t) {
         const int it = snake(cl, t, ncl);
-        if (it >= p.n_items) break;
+        if (it >= n_items) break;
         const TileItem ti = p.items[it];
         const MatDesc d = p.descs[ti.mat];
         const int bn = tc2_cfg_bn(d.cfg);
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       bool ok = true;
       for (int t = 0; ok; ++t) {
         const int it = snake(cl, t, ncl);
-        if (it >= p.n_items) break;
+        if (it >= n_items) break;
         const TileItem ti = p.items[it];
         const MatDesc d = p.descs[ti.mat];
         const int bn = tc2_cfg_bn(d.cfg);
@@ -243,17 +245,18 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
     const float alpha = p.alpha, beta = p.beta;
     for (int t = 0;; ++t) {
       const int it = snake(cl, t, ncl);
-      if (it >= p.n_items) break;
+      if (it >= n_items) break;
       const TileItem ti = p.items[it];
       const MatDesc d = p.descs[ti.mat];
       float* C = p.C[ti.mat];
       const int bn = tc2_cfg_bn(d.cfg);
       const bool swap = tc_cfg_swap(d.cfg);
-      const int row = ti.tm * 256 + (int)rank * kRows + q * 32 + lane;  // A-side row
+      const int row0 = ti.tm * 256 + (int)rank * kRows + q * 32;  // A-side row of lane 0
       const long long ldc = d.ldc;
       const int c_lo = half * kCols;
       const int ncols = max(0, min(kCols, bn - c_lo));
       const int col_base = ti.tn * bn + c_lo;
+      if (beta != 0.0f) c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
       const int nk = (d.K + KE - 1) / KE;
       const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
       const int ngroups = (d.K <= kFineK2) ? nsub : nk;
@@ -287,17 +290,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
         acc.next(kNAcc);
       }
       if (!ok) break;
-#pragma unroll
-      for (int j = 0; j < kCols; ++j) {
-        if (j < ncols) {
-          const int m = swap ? col_base + j : row;
-          const int n = swap ? row : col_base + j;
-          if (m < d.M && n < d.N) {
-            float* c = C + m + n * ldc;
-            *c = (beta == 0.0f) ? alpha * r[j] : fmaf(alpha, r[j], beta * *c);
-          }
-        }
-      }
+      c_store<kCols>(r, C, ldc, d.M, d.N, swap, row0, col_base, ncols, alpha, beta, lane);
     }
   }
 

@@ -22,6 +22,7 @@
 // for an accumulator group to promote, and do whichever is ready.
 #include <stdint.h>
 
+#include "tc_epilogue.h"
 #include "tc_ptx.h"
 
 namespace bgemm {
@@ -81,6 +82,7 @@ __global__ void __launch_bounds__(kThreadsS, 1) tc2s_gemm_kernel(const TcGemmPar
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
+  const int n_items = p.n_items_dev ? *p.n_items_dev : p.n_items;
   const uint32_t rank = cluster_ctarank();
   const bool leader = rank == 0;
   const int cl = blockIdx.x >> 1;
@@ -125,7 +127,7 @@ __global__ void __launch_bounds__(kThreadsS, 1) tc2s_gemm_kernel(const TcGemmPar
       int last_mat = -1;
       for (int t = 0; ok; ++t) {
         const int it = snake(cl, t, ncl);
-        if (it >= p.n_items) break;
+        if (it >= n_items) break;
         const TileItem ti = p.items[it];
         const MatDesc d = p.descs[ti.mat];
         const int bn = tc2_cfg_bn(d.cfg);
@@ -166,7 +168,7 @@ __global__ void __launch_bounds__(kThreadsS, 1) tc2s_gemm_kernel(const TcGemmPar
       bool ok = true;
       for (int t = 0; ok; ++t) {
         const int it = snake(cl, t, ncl);
-        if (it >= p.n_items) break;
+        if (it >= n_items) break;
         const TileItem ti = p.items[it];
         const MatDesc d = p.descs[ti.mat];
         const int bn = tc2_cfg_bn(d.cfg);
@@ -245,7 +247,7 @@ __global__ void __launch_bounds__(kThreadsS, 1) tc2s_gemm_kernel(const TcGemmPar
     auto conv_tile = [&]() {  // advance to the next tile that has K > 0
       for (;;) {
         const int it = snake(cl, ct, ncl);
-        if (it >= p.n_items) { conv_done = true; return; }
+        if (it >= n_items) { conv_done = true; return; }
         const MatDesc d = p.descs[p.items[it].mat];
         c_nk = (d.K + KE - 1) / KE;
         c_hb = tc2_cfg_bn(d.cfg) >> 1;
@@ -263,7 +265,7 @@ __global__ void __launch_bounds__(kThreadsS, 1) tc2s_gemm_kernel(const TcGemmPar
     MatDesc pd{};
     auto prom_tile = [&]() {
       const int it = snake(cl, pt, ncl);
-      if (it >= p.n_items) { prom_done = true; return; }
+      if (it >= n_items) { prom_done = true; return; }
       pti = p.items[it];
       pd = p.descs[pti.mat];
       const int nk = (pd.K + KE - 1) / KE;
@@ -282,24 +284,15 @@ __global__ void __launch_bounds__(kThreadsS, 1) tc2s_gemm_kernel(const TcGemmPar
       while (!prom_done && pg == p_ng) {
         const int bn = tc2_cfg_bn(pd.cfg);
         const bool swap = tc_cfg_swap(pd.cfg);
-        const int row = pti.tm * 256 + (int)rank * kRows + q * 32 + lane;
+        const int row0 = pti.tm * 256 + (int)rank * kRows + q * 32;
         const int c_lo = half * kCols;
         const int ncols = max(0, min(kCols, bn - c_lo));
         const int col_base = pti.tn * bn + c_lo;
         float* C = p.C[pti.mat];
         const long long ldc = pd.ldc;
+        c_store<kCols>(r, C, ldc, pd.M, pd.N, swap, row0, col_base, ncols, alpha, beta, lane);
 #pragma unroll
-        for (int j = 0; j < kCols; ++j) {
-          if (j < ncols) {
-            const int m = swap ? col_base + j : row;
-            const int n = swap ? row : col_base + j;
-            if (m < pd.M && n < pd.N) {
-              float* c = C + m + n * ldc;
-              *c = (beta == 0.0f) ? alpha * r[j] : fmaf(alpha, r[j], beta * *c);
-            }
-          }
-          r[j] = 0.0f;
-        }
+        for (int j = 0; j < kCols; ++j) r[j] = 0.0f;
         ++pt;
         prom_tile();
       }

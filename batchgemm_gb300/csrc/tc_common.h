@@ -51,6 +51,7 @@ struct TcPackParams {
   const PackDesc* pdescs;
   const PackJob* jobs;
   int n_jobs;
+  const int* n_jobs_dev;  // if set, the job count is read from the device
   int kind;
   int split;
   char* ws;
@@ -62,6 +63,7 @@ struct TcGemmParams {
   const MatDesc* descs;
   const TileItem* items;
   int n_items;
+  const int* n_items_dev;      // if set, the item count is read from the device
   int* counters;               // [0] queue head, [1] CTAs finished
   const CUtensorMap* tmaps;    // 4 per matrix: A-side hi, A-side lo, B-side hi, B-side lo
   float alpha, beta;

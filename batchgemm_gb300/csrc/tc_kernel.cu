@@ -39,6 +39,7 @@
 // form; this file is the new precision path that the tile queue drives.
 #include <stdint.h>
 
+#include "tc_epilogue.h"
 #include "tc_ptx.h"
 
 namespace bgemm {
@@ -130,7 +131,8 @@ __device__ __forceinline__ void put4(char* hi, char* lo, long long idx, const fl
 __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
   __shared__ float t[64][33];
   const int tid = threadIdx.x;
-  for (int j = blockIdx.x; j < p.n_jobs; j += gridDim.x) {
+  const int n_jobs = p.n_jobs_dev ? *p.n_jobs_dev : p.n_jobs;
+  for (int j = blockIdx.x; j < n_jobs; j += gridDim.x) {
     const PackJob job = p.jobs[j];
     const MatDesc d = p.descs[job.mat];
     const PackDesc pd = p.pdescs[job.mat];
@@ -281,6 +283,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
+  const int n_items = p.n_items_dev ? *p.n_items_dev : p.n_items;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
@@ -319,10 +322,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
       for (;;) {
         const int it = atomicAdd(p.counters, 1);
         if (!wait_bounded(sempty(sc.idx), sc.phase ^ 1u, p.error, abort, p.timeout_ns)) break;
-        slots[sc.idx] = (it < p.n_items) ? it : -1;
+        slots[sc.idx] = (it < n_items) ? it : -1;
         mbar_arrive(sfull(sc.idx));
         sc.next(kSchedSlots);
-        if (it >= p.n_items) break;
+        if (it >= n_items) break;
         const TileItem ti = p.items[it];
         const MatDesc d = p.descs[ti.mat];
         const int bn = tc_cfg_bn(d.cfg);
@@ -492,11 +495,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
       float* C = p.C[ti.mat];
       const int bn = tc_cfg_bn(d.cfg);
       const bool swap = tc_cfg_swap(d.cfg);
-      const int row = ti.tm * kTcBM + q * 32 + lane;  // A-side row
+      const int row0 = ti.tm * kTcBM + q * 32;        // A-side row of lane 0
       const long long ldc = d.ldc;
       const int c_lo = half * kEpiCols;               // first accumulator column owned
       const int ncols = max(0, min(kEpiCols, bn - c_lo));
       const int col_base = ti.tn * bn + c_lo;         // B-side index of owned column 0
+      if (beta != 0.0f) c_prefetch<kEpiCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
       float r[kEpiCols];
 #pragma unroll
       for (int j = 0; j < kEpiCols; ++j) r[j] = 0.0f;
@@ -547,17 +551,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
         if (lane == 0) mbar_arrive(tempty(acc.idx));
         acc.next(NACC);
       }
-#pragma unroll
-      for (int j = 0; j < kEpiCols; ++j) {
-        if (j < ncols) {
-          const int m = swap ? col_base + j : row;
-          const int n = swap ? row : col_base + j;
-          if (m < d.M && n < d.N) {
-            float* c = C + m + n * ldc;
-            *c = (beta == 0.0f) ? alpha * r[j] : fmaf(alpha, r[j], beta * *c);
-          }
-        }
-      }
+      c_store<kEpiCols>(r, C, ldc, d.M, d.N, swap, row0, col_base, ncols, alpha, beta, lane);
     }
   }
 
@@ -599,7 +593,7 @@ cudaError_t tc_tmap_launch(const TcTmapParams& p, cudaStream_t s) {
 }
 
 cudaError_t tc_pack_launch(const TcPackParams& p, int grid, cudaStream_t s) {
-  if (p.n_jobs == 0) return cudaSuccess;
+  if (p.n_jobs == 0 && !p.n_jobs_dev) return cudaSuccess;
   tc_pack_kernel<<<grid, 256, 0, s>>>(p);
   return cudaGetLastError();
 }

@@ -16,26 +16,35 @@ namespace bgemm {
 
 struct TcPlan {
   int kind = kKindTF32;
-  int split = 1;
-  int nprod = 3;
+  int split = 1;             // the kernels read hi/lo pairs (kind TF32/BF16 split modes)
+  bool split_mode = true;    // the plan's mode is TF32X3 or BF16X3
+  int want_family = 0;       // 0: cost model, 1: one-SM, 2: CTA pair
+  bool raw_ok = false;       // TF32X3 with the in-kernel split requested
+  bool pair = false;         // CTA-pair kernel (tc2_kernel.cu)
+  bool raw = false;          // 3xTF32 on pairs: raw FP32 operands split in the kernel
+  int clusters = 0;          // CTA pairs resident at once
+  bool host_tmaps = false;   // encode every tensor map on the host (comparison path)
+  // capacity and device memory
+  int cap_batch = 0, cap_jobs = 0;
+  size_t cap_ws = 0;
   void* d_ws = nullptr;      // split operands
-  size_t ws_bytes = 0;
-  void* d_mem = nullptr;     // tensor maps | pack descs | jobs | error word
-  void* h_pin = nullptr;
+  void* d_mem = nullptr;     // templates | tensor maps | pack descs | jobs | error word
+  void* h_stage[2] = {nullptr, nullptr};  // pinned staging, same layout as d_mem
+  size_t off_tm = 0, off_pd = 0, off_jobs = 0, off_err = 0, mem_bytes = 0;
+  CUtensorMap* d_templ = nullptr;
   CUtensorMap* d_tmaps = nullptr;
   PackDesc* d_pdescs = nullptr;
   PackJob* d_jobs = nullptr;
   int* d_err = nullptr;
   int n_jobs = 0;
   int pack_grid = 1;
-  bool pair = false;   // CTA-pair kernel (tc2_kernel.cu)
-  int clusters = 0;    // CTA pairs resident at once
-  bool host_tmaps = false;  // encode every tensor map on the host (comparison path)
-  bool split_in_kernel = false;  // 3xTF32 on pairs: split raw FP32 in shared memory
-  bool raw = false;         // 3xTF32 on pairs: raw FP32 operands split in the kernel
+  // layout of the last planned batch, uploaded by tc_commit
+  std::vector<PackDesc> pd;
+  std::vector<PackJob> jobs;
 };
 
 static inline long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
+static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 static int g_mode = BGEMM_MODE_TF32X3;
 static bool g_pair = false;
@@ -57,37 +66,51 @@ static bool tc_eval(int c, int M, int N, int K, long long* tiles, double* t_tile
   return true;
 }
 
-bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int* K, int batch,
-                         const bgemm_plan_options_t* opt, std::vector<MatPlan>& mp) {
+bgemm_status_t tc_init(bgemm_plan_s* p, const bgemm_plan_options_t* opt) {
   auto* t = new TcPlan();
-  t->kind = (p->mode == BGEMM_MODE_BF16X3) ? kKindBF16 : kKindTF32;
-  t->split = (p->mode == BGEMM_MODE_TF32) ? 0 : 1;
-  t->nprod = t->split ? 3 : 1;
-  t->host_tmaps = opt && opt->host_tensor_maps;
-  t->split_in_kernel = opt && opt->split_in_kernel;
   p->tc = t;
-  if (opt && opt->force_tile_config >= 0)
-    t->pair = tc_cfg_pair(opt->force_tile_config);
-  else
-    t->pair = t->split;  // candidate; the cost comparison below decides
-  if (t->pair && !t->split)
-    return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1,
-                     "CTA-pair tiles serve the split modes only");
-  if (t->pair) {
-    const bool raw_ok = p->mode == BGEMM_MODE_TF32X3 && t->split_in_kernel;
-    t->clusters = raw_ok ? tc2s_max_clusters() : tc2_max_clusters();
-    if (t->clusters < 1) {
-      if (opt && opt->force_tile_config >= 0)
-        return set_error(BGEMM_ERROR_NOT_SUPPORTED, 11, -1, "no CTA pair fits on this device");
-      t->pair = false;
-    }
+  t->kind = (p->mode == BGEMM_MODE_BF16X3) ? kKindBF16 : kKindTF32;
+  t->split_mode = p->mode != BGEMM_MODE_TF32;
+  t->split = t->split_mode ? 1 : 0;
+  t->host_tmaps = opt->host_tensor_maps != 0;
+  t->raw_ok = p->mode == BGEMM_MODE_TF32X3 && opt->split_in_kernel;
+  int fam = opt->kernel_family;
+  if (fam < 0 || fam > 2)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1, "kernel_family %d is not 0, 1 or 2", fam);
+  if (opt->force_tile_config >= 0) {
+    const int forced = tc_cfg_pair(opt->force_tile_config) ? 2 : 1;
+    if (fam != 0 && fam != forced)
+      return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1,
+                       "force_tile_config %d belongs to kernel family %d, not %d",
+                       opt->force_tile_config, forced, fam);
+    fam = forced;
   }
+  if (fam == 2 && !t->split_mode)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1, "CTA-pair tiles serve the split modes only");
+  if (t->split_mode) t->clusters = t->raw_ok ? tc2s_max_clusters() : tc2_max_clusters();
+  if (fam == 2 && t->clusters < 1)
+    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 11, -1, "no CTA pair fits on this device");
+  t->want_family = fam;
+  return BGEMM_SUCCESS;
+}
+
+bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int* K, int batch,
+                         bool first, std::vector<MatPlan>& mp) {
+  TcPlan* t = p->tc;
+  const bgemm_plan_options_t* opt = &p->opt;
   static std::mutex mu;
   std::lock_guard<std::mutex> lk(mu);
   g_mode = p->mode;
   const int single_slots = p->facts.num_sms * p->facts.tc_ctas_per_sm;
-  const bool forced = opt && opt->force_tile_config >= 0;
-  if (!forced && t->split && t->clusters > 0) {
+  if (!first) {
+    g_pair = t->pair;
+    return choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, t->pair ? t->clusters : single_slots,
+                        opt, mp);
+  }
+  int fam = t->want_family;
+  if (fam == 0 && (!t->split_mode || t->clusters < 1)) fam = 1;
+  bgemm_status_t st = BGEMM_SUCCESS;
+  if (fam == 0) {
     // plan both kernels with the cost table and keep the shorter makespan
     auto makespan = [&](const std::vector<MatPlan>& v, int slots) {
       double total = 0, longest = 0;
@@ -104,18 +127,22 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
     g_pair = true;
     bgemm_status_t s2 = choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, t->clusters, opt, two);
     if (s1 != BGEMM_SUCCESS && s2 != BGEMM_SUCCESS) return s1;
-    const bool pair = s2 == BGEMM_SUCCESS &&
-                      (s1 != BGEMM_SUCCESS ||
-                       makespan(two, t->clusters) < makespan(one, single_slots));
-    t->pair = pair;
-    mp = pair ? two : one;
-    t->raw = t->pair && p->mode == BGEMM_MODE_TF32X3 && t->split_in_kernel;
-    return BGEMM_SUCCESS;
+    t->pair = s2 == BGEMM_SUCCESS &&
+              (s1 != BGEMM_SUCCESS || makespan(two, t->clusters) < makespan(one, single_slots));
+    mp = t->pair ? two : one;
+  } else {
+    t->pair = fam == 2;
+    g_pair = t->pair;
+    st = choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, t->pair ? t->clusters : single_slots,
+                      opt, mp);
   }
-  g_pair = t->pair;
-  t->raw = t->pair && p->mode == BGEMM_MODE_TF32X3 && t->split_in_kernel;
-  const int slots = t->pair ? t->clusters : single_slots;
-  return choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, slots, opt, mp);
+  t->raw = t->pair && t->raw_ok;
+  if (t->raw) {
+    // 3xTF32 on CTA pairs: compact raw FP32 operands, split in the kernel
+    t->kind = kKindRaw;
+    t->split = 0;
+  }
+  return st;
 }
 
 void tc_tile_dims(bgemm_plan_s* p, int, int, int, int cfg, int* bm, int* bn, MatDesc* d) {
@@ -125,7 +152,43 @@ void tc_tile_dims(bgemm_plan_s* p, int, int, int, int cfg, int* bm, int* bn, Mat
   d->aux = tc_cfg_swap(cfg) ? kTcSwapFlag : 0;
 }
 
-size_t tc_extra_bytes(bgemm_plan_s*, int) { return 0; }
+// Workspace: per matrix [A hi][A lo][B hi][B lo], rows of kpad elements;
+// pack jobs: strips of 32 rows, matrices with the longest K first.
+void tc_layout(bgemm_plan_s* p, const std::vector<MatDesc>& hd, bgemm_plan_requirements_t* req) {
+  TcPlan* t = p->tc;
+  const int batch = (int)hd.size();
+  const int esz = (t->kind == kKindBF16) ? 2 : 4;
+  t->pd.assign(batch, PackDesc{});
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += align256(bytes);
+    return (long long)o;
+  };
+  for (int i = 0; i < batch; ++i) {
+    const MatDesc& d = hd[i];
+    PackDesc& q = t->pd[i];
+    q.kpad = (int)((d.K + (16 / esz) - 1) / (16 / esz) * (16 / esz));
+    if (d.M == 0 || d.N == 0 || d.K == 0) continue;
+    const size_t a = (size_t)d.M * q.kpad * esz, b = (size_t)d.N * q.kpad * esz;
+    q.a_hi = take(a);
+    q.a_lo = t->split ? take(a) : q.a_hi;
+    q.b_hi = take(b);
+    q.b_lo = t->split ? take(b) : q.b_hi;
+  }
+  std::vector<int> order;
+  for (int i = 0; i < batch; ++i)
+    if (hd[i].M > 0 && hd[i].N > 0 && hd[i].K > 0) order.push_back(i);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hd[a].K > hd[b].K; });
+  t->jobs.clear();
+  for (int i : order) {
+    for (int r = 0; r < hd[i].M; r += 32) t->jobs.push_back(PackJob{i, 0, r, 0});
+    for (int r = 0; r < hd[i].N; r += 32) t->jobs.push_back(PackJob{i, 1, r, 0});
+  }
+  req->pack_jobs = (int)std::min<size_t>(t->jobs.size(), (size_t)1 << 30);
+  req->workspace_bytes = std::max<size_t>(off, 256);
+  req->kernel_family = t->pair ? 2 : 1;
+}
 
 // ----------------------------------------------------------- tensor maps --
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -160,80 +223,51 @@ static bool encode_panel(CUtensorMap* out, int kind, void* base, int K, int rows
   return r == CUDA_SUCCESS;
 }
 
-bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream) {
+// The four maps of matrix i (A-side hi/lo, B-side hi/lo) encoded on the host.
+static bool encode_matrix_maps(const TcPlan* t, const MatDesc& d, const PackDesc& q, char* ws,
+                               CUtensorMap* out) {
+  const bool swap = tc_cfg_swap(d.cfg);
+  // one SM: A-side boxes of 128 rows, B-side boxes of bn rows; a CTA pair
+  // loads per CTA 128 A-side rows and half of the bn B-side rows
+  const int bbox = t->pair ? tc2_cfg_bn(d.cfg) / 2 : tc_cfg_bn(d.cfg);
+  const long long off[4] = {swap ? q.b_hi : q.a_hi, swap ? q.b_lo : q.a_lo,
+                            swap ? q.a_hi : q.b_hi, swap ? q.a_lo : q.b_lo};
+  const int rows[4] = {swap ? d.N : d.M, swap ? d.N : d.M, swap ? d.M : d.N, swap ? d.M : d.N};
+  for (int part = 0; part < 4; ++part)
+    if (!encode_panel(&out[part], t->kind, ws + off[part], d.K, rows[part], q.kpad,
+                      part < 2 ? kTcBM : bbox))
+      return false;
+  return true;
+}
+
+bgemm_status_t tc_alloc(bgemm_plan_s* p) {
   TcPlan* t = p->tc;
-  const int batch = p->batch;
-  if (t->raw) {
-    // 3xTF32 on CTA pairs: compact raw FP32 operands, split in the kernel
-    t->kind = kKindRaw;
-    t->split = 0;
-  }
-  const int esz = (t->kind == kKindBF16) ? 2 : 4;
-  const int parts = t->split ? 2 : 1;
-  const std::vector<MatDesc>& hd = p->host_descs;
+  t->cap_batch = p->cap.batch;
+  t->cap_jobs = p->cap.pack_jobs;
+  t->cap_ws = std::max<size_t>(p->cap.workspace_bytes, 256);
+  t->off_tm = sizeof(CUtensorMap) * 2 * kTmapBoxClasses;  // templates first
+  t->off_pd = t->off_tm + sizeof(CUtensorMap) * 4 * (size_t)t->cap_batch;
+  t->off_jobs = t->off_pd + align256(sizeof(PackDesc) * (size_t)t->cap_batch);
+  t->off_err = t->off_jobs + align256(sizeof(PackJob) * (size_t)t->cap_jobs);
+  t->mem_bytes = t->off_err + 256;
 
-  // workspace layout: per matrix [A hi][A lo][B hi][B lo], rows of kpad
-  std::vector<PackDesc> pd(batch);
-  size_t off = 0;
-  auto take = [&](size_t bytes) {
-    const size_t o = off;
-    off += (bytes + 255) & ~size_t(255);
-    return (long long)o;
-  };
-  for (int i = 0; i < batch; ++i) {
-    const MatDesc& d = hd[i];
-    PackDesc& q = pd[i];
-    std::memset(&q, 0, sizeof(q));
-    q.kpad = (int)((d.K + (16 / esz) - 1) / (16 / esz) * (16 / esz));
-    if (d.M == 0 || d.N == 0 || d.K == 0) continue;
-    const size_t a = (size_t)d.M * q.kpad * esz, b = (size_t)d.N * q.kpad * esz;
-    q.a_hi = take(a);
-    q.a_lo = t->split ? take(a) : q.a_hi;
-    q.b_hi = take(b);
-    q.b_lo = t->split ? take(b) : q.b_hi;
-  }
-  t->ws_bytes = std::max<size_t>(off, 256);
-  (void)parts;
-
-  // pack jobs: strips of 32 rows, matrices with the longest K first
-  std::vector<int> order;
-  for (int i = 0; i < batch; ++i)
-    if (hd[i].M > 0 && hd[i].N > 0 && hd[i].K > 0) order.push_back(i);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hd[a].K > hd[b].K; });
-  std::vector<PackJob> jobs;
-  for (int i : order) {
-    for (int r = 0; r < hd[i].M; r += 32) jobs.push_back(PackJob{i, 0, r, 0});
-    for (int r = 0; r < hd[i].N; r += 32) jobs.push_back(PackJob{i, 1, r, 0});
-  }
-  t->n_jobs = (int)jobs.size();
-  t->pack_grid = (int)std::max<long long>(1, std::min<long long>(t->n_jobs,
-                                                                 (long long)p->facts.num_sms * 8));
-
-  const size_t off_tpl = 0;  // template maps for the device-side build
-  const size_t off_tm = off_tpl + sizeof(CUtensorMap) * 2 * kTmapBoxClasses;
-  const size_t off_pd = off_tm + sizeof(CUtensorMap) * 4 * (size_t)batch;
-  const size_t off_jobs = off_pd + ((sizeof(PackDesc) * (size_t)batch + 255) & ~size_t(255));
-  const size_t off_err = off_jobs + ((sizeof(PackJob) * jobs.size() + 255) & ~size_t(255));
-  const size_t total = off_err + 256;
-
-  cudaError_t e = cudaMalloc(&t->d_ws, t->ws_bytes);
+  cudaError_t e = cudaMalloc(&t->d_ws, t->cap_ws);
   if (e != cudaSuccess)
     return set_error(BGEMM_ERROR_ALLOC, 0, -1, "split-operand workspace of %zu bytes: %s",
-                     t->ws_bytes, cudaGetErrorString(e));
-  e = cudaMalloc(&t->d_mem, total);
-  if (e == cudaSuccess) e = cudaMallocHost(&t->h_pin, total);
+                     t->cap_ws, cudaGetErrorString(e));
+  e = cudaMalloc(&t->d_mem, t->mem_bytes);
+  for (int s = 0; s < 2 && e == cudaSuccess; ++s) e = cudaMallocHost(&t->h_stage[s], t->mem_bytes);
   if (e != cudaSuccess)
     return set_error(BGEMM_ERROR_ALLOC, 0, -1, "tensor-core plan memory: %s",
                      cudaGetErrorString(e));
-  char* h = static_cast<char*>(t->h_pin);
-  std::memset(h, 0, total);
-  auto* tm = reinterpret_cast<CUtensorMap*>(h + off_tm);
-  char* ws = static_cast<char*>(t->d_ws);
+  for (int s = 0; s < 2; ++s) std::memset(t->h_stage[s], 0, t->mem_bytes);
   {
     // templates per (box height, extent class); the device patches one copy
     // per operand panel (address, dims, row stride)
+    const int esz = (t->kind == kKindBF16) ? 2 : 4;
     const int ke = 128 / esz;
-    auto* tpl = reinterpret_cast<CUtensorMap*>(h + off_tpl);
+    auto* tpl = static_cast<CUtensorMap*>(t->h_stage[0]);
+    void* ws = t->d_ws;
     for (int b = 16; b <= 128; b *= 2) {
       const bool ok = encode_panel(&tpl[tmap_template_index(b, false)], t->kind, ws, ke, kTcBM, ke,
                                    b) &&  // 128 rows x 128 B = 16 KiB
@@ -242,48 +276,63 @@ bgemm_status_t tc_plan_finish(bgemm_plan_s* p, cudaStream_t stream) {
       if (!ok) return set_error(BGEMM_ERROR_INTERNAL, 0, -1, "template tensor map encoding failed");
     }
   }
-  for (int i = 0; i < batch && t->host_tmaps; ++i) {
-    const MatDesc& d = hd[i];
-    if (d.M == 0 || d.N == 0 || d.K == 0) continue;
-    const bool swap = tc_cfg_swap(d.cfg);
-    // one SM: A-side boxes of 128 rows, B-side boxes of bn rows; a CTA pair
-    // loads per CTA 128 A-side rows and half of the bn B-side rows
-    const int bbox = t->pair ? tc2_cfg_bn(d.cfg) / 2 : tc_cfg_bn(d.cfg);
-    const PackDesc& q = pd[i];
-    const long long sa_hi = swap ? q.b_hi : q.a_hi, sa_lo = swap ? q.b_lo : q.a_lo;
-    const long long sb_hi = swap ? q.a_hi : q.b_hi, sb_lo = swap ? q.a_lo : q.b_lo;
-    const int ra = swap ? d.N : d.M, rb = swap ? d.M : d.N;
-    bool ok = encode_panel(&tm[4 * i + 0], t->kind, ws + sa_hi, d.K, ra, q.kpad, kTcBM) &&
-              encode_panel(&tm[4 * i + 1], t->kind, ws + sa_lo, d.K, ra, q.kpad, kTcBM) &&
-              encode_panel(&tm[4 * i + 2], t->kind, ws + sb_hi, d.K, rb, q.kpad, bbox) &&
-              encode_panel(&tm[4 * i + 3], t->kind, ws + sb_lo, d.K, rb, q.kpad, bbox);
-    if (!ok)
-      return set_error(BGEMM_ERROR_INTERNAL, 0, i, "tensor map encoding failed for matrix %d", i);
-  }
-  std::memcpy(h + off_pd, pd.data(), sizeof(PackDesc) * (size_t)batch);
-  if (!jobs.empty()) std::memcpy(h + off_jobs, jobs.data(), sizeof(PackJob) * jobs.size());
   char* dm = static_cast<char*>(t->d_mem);
-  t->d_tmaps = reinterpret_cast<CUtensorMap*>(dm + off_tm);
-  t->d_pdescs = reinterpret_cast<PackDesc*>(dm + off_pd);
-  t->d_jobs = reinterpret_cast<PackJob*>(dm + off_jobs);
-  t->d_err = reinterpret_cast<int*>(dm + off_err);
-  e = cudaMemcpyAsync(t->d_mem, t->h_pin, total, cudaMemcpyHostToDevice, stream);
-  if (e != cudaSuccess) return cuda_error(e, "tensor-core descriptor upload");
-  if (!t->host_tmaps) {
-    // per-matrix tensor maps built on the device, once per plan
-    TcTmapParams tp{p->d_descs, t->d_pdescs, reinterpret_cast<CUtensorMap*>(dm + off_tpl),
-                    t->d_tmaps, ws, batch, t->kind, t->pair ? 1 : 0};
-    e = tc_tmap_launch(tp, stream);
-    if (e != cudaSuccess) return cuda_error(e, "tensor-map build launch");
-  }
-  p->info.workspace_bytes = t->ws_bytes;
-  p->info.device_bytes += t->ws_bytes + total;
+  t->d_templ = reinterpret_cast<CUtensorMap*>(dm);
+  t->d_tmaps = reinterpret_cast<CUtensorMap*>(dm + t->off_tm);
+  t->d_pdescs = reinterpret_cast<PackDesc*>(dm + t->off_pd);
+  t->d_jobs = reinterpret_cast<PackJob*>(dm + t->off_jobs);
+  t->d_err = reinterpret_cast<int*>(dm + t->off_err);
+  t->pack_grid = (int)std::max<long long>(
+      1, std::min<long long>(t->cap_jobs, (long long)p->facts.num_sms * 8));
+  p->info.workspace_bytes = t->cap_ws;
+  p->info.device_bytes += t->cap_ws + t->mem_bytes;
   p->info.kernels_per_execute = 2;
   if (t->pair) {
     // one CTA pair per cluster slot, never more pairs than tiles
-    const int pairs = std::max(1, std::min(t->clusters, std::max(p->n_items, 1)));
+    const int pairs = std::max(1, std::min(t->clusters, std::max(p->cap.tiles, 1)));
     p->grid = 2 * pairs;
     p->info.grid = p->grid;
+  }
+  return BGEMM_SUCCESS;
+}
+
+bgemm_status_t tc_commit(bgemm_plan_s* p, int stage, int batch, bool first, cudaStream_t stream) {
+  TcPlan* t = p->tc;
+  char* h = static_cast<char*>(t->h_stage[stage]);
+  char* dm = static_cast<char*>(t->d_mem);
+  char* ws = static_cast<char*>(t->d_ws);
+  if (batch > 0) std::memcpy(h + t->off_pd, t->pd.data(), sizeof(PackDesc) * (size_t)batch);
+  if (!t->jobs.empty())
+    std::memcpy(h + t->off_jobs, t->jobs.data(), sizeof(PackJob) * t->jobs.size());
+  if (t->host_tmaps) {
+    auto* tm = reinterpret_cast<CUtensorMap*>(h + t->off_tm);
+    for (int i = 0; i < batch; ++i) {
+      const MatDesc& d = p->host_descs[i];
+      if (d.M == 0 || d.N == 0 || d.K == 0) continue;
+      if (!encode_matrix_maps(t, d, t->pd[i], ws, &tm[4 * i]))
+        return set_error(BGEMM_ERROR_INTERNAL, 0, i, "tensor map encoding failed for matrix %d", i);
+    }
+  }
+  auto copy = [&](size_t off, size_t bytes) {
+    return bytes ? cudaMemcpyAsync(dm + off, h + off, bytes, cudaMemcpyHostToDevice, stream)
+                 : cudaSuccess;
+  };
+  cudaError_t e = cudaSuccess;
+  if (first) {
+    e = copy(0, t->off_tm);  // templates
+    if (e == cudaSuccess) e = copy(t->off_err, 256);  // zero error word
+  }
+  if (e == cudaSuccess && t->host_tmaps) e = copy(t->off_tm, sizeof(CUtensorMap) * 4 * (size_t)batch);
+  if (e == cudaSuccess) e = copy(t->off_pd, sizeof(PackDesc) * (size_t)batch);
+  if (e == cudaSuccess) e = copy(t->off_jobs, sizeof(PackJob) * t->jobs.size());
+  if (e != cudaSuccess) return cuda_error(e, "tensor-core descriptor upload");
+  t->n_jobs = (int)t->jobs.size();
+  if (!t->host_tmaps && batch > 0) {
+    // per-matrix tensor maps built on the device, once per batch
+    TcTmapParams tp{p->d_descs, t->d_pdescs, t->d_templ, t->d_tmaps, ws, batch, t->kind,
+                    t->pair ? 1 : 0};
+    e = tc_tmap_launch(tp, stream);
+    if (e != cudaSuccess) return cuda_error(e, "tensor-map build launch");
   }
   return BGEMM_SUCCESS;
 }
@@ -308,19 +357,10 @@ int tc_debug_compare_tmaps(bgemm_plan_s* p, cudaStream_t stream, int* n_maps, in
   for (int i = 0; i < batch; ++i) {
     const MatDesc& d = p->host_descs[i];
     if (d.M == 0 || d.N == 0 || d.K == 0) continue;
-    const bool swap = tc_cfg_swap(d.cfg);
-    const int bbox = t->pair ? tc2_cfg_bn(d.cfg) / 2 : tc_cfg_bn(d.cfg);
-    const PackDesc& q = pd[i];
-    const long long off[4] = {swap ? q.b_hi : q.a_hi, swap ? q.b_lo : q.a_lo,
-                              swap ? q.a_hi : q.b_hi, swap ? q.a_lo : q.b_lo};
-    const int rows[4] = {swap ? d.N : d.M, swap ? d.N : d.M, swap ? d.M : d.N, swap ? d.M : d.N};
+    if (!encode_matrix_maps(t, d, pd[i], ws, &host[4 * i])) return -1;
     for (int part = 0; part < 4; ++part) {
-      CUtensorMap& h = host[4 * i + part];
-      if (!encode_panel(&h, t->kind, ws + off[part], d.K, rows[part], q.kpad,
-                        part < 2 ? kTcBM : bbox))
-        return -1;
       ++maps;
-      const unsigned char* a = reinterpret_cast<const unsigned char*>(&h);
+      const unsigned char* a = reinterpret_cast<const unsigned char*>(&host[4 * i + part]);
       const unsigned char* b = reinterpret_cast<const unsigned char*>(&dev[4 * i + part]);
       for (int k = 0; k < (int)sizeof(CUtensorMap); ++k)
         if (a[k] != b[k]) {
@@ -340,12 +380,12 @@ bgemm_status_t tc_execute(bgemm_plan_s* p, float alpha, const float* const* dA,
                           const float* const* dB, float beta, float* const* dC,
                           cudaStream_t stream) {
   TcPlan* t = p->tc;
-  TcPackParams pp{p->d_descs, t->d_pdescs, t->d_jobs, t->n_jobs, t->kind, t->split,
-                  static_cast<char*>(t->d_ws), dA, dB};
+  TcPackParams pp{p->d_descs, t->d_pdescs,  t->d_jobs, t->n_jobs, p->d_counters + kHdrJobs,
+                  t->kind,       t->split,      static_cast<char*>(t->d_ws), dA, dB};
   cudaError_t e = tc_pack_launch(pp, t->pack_grid, stream);
   if (e != cudaSuccess) return cuda_error(e, "split/pack launch");
-  TcGemmParams gp{p->d_descs, p->d_items, p->n_items, p->d_counters, t->d_tmaps, alpha, beta,
-                  dC, t->d_err, 2000000000ull};
+  TcGemmParams gp{p->d_descs, p->d_items, p->n_items, p->d_counters + kHdrItems,
+                  p->d_counters, t->d_tmaps, alpha, beta, dC, t->d_err, 2000000000ull};
   if (p->ev_start) cudaEventRecord(p->ev_start, stream);
   e = t->raw    ? tc2s_gemm_launch(gp, p->grid, stream)
       : t->pair ? tc2_gemm_launch(t->kind, gp, p->grid, stream)
@@ -373,7 +413,8 @@ void tc_plan_release(bgemm_plan_s* p) {
   if (!t) return;
   if (t->d_ws) cudaFree(t->d_ws);
   if (t->d_mem) cudaFree(t->d_mem);
-  if (t->h_pin) cudaFreeHost(t->h_pin);
+  for (void* h : t->h_stage)
+    if (h) cudaFreeHost(h);
   delete t;
   p->tc = nullptr;
 }

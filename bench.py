@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the other modes")
+    ap.add_argument("--no-stream", action="store_true", help="skip the batch-stream leg")
+    ap.add_argument("--stream-batches", type=int, default=200)
     return ap.parse_args()
 
 
@@ -195,8 +197,9 @@ def cpu_sample(w, budget_s=15.0, threads=None):
 
 
 # ---------------------------------------------------------------- GPU leg --
-def fp64_sampled_error(db, per_matrix=4, seed=0):
-    """Normalised error |c - c64| / sum|a b| on sampled entries, FP64 on the GPU."""
+def fp64_sampled_error(db, per_matrix=4, seed=0, C0=None, beta=0.0):
+    """Normalised error |c - c64| / (sum|a b| + |beta c0|) on sampled entries,
+    FP64 on the GPU (C0: the C buffer before the step, when beta != 0)."""
     import torch
     rng = np.random.default_rng(seed)
     idx_m, idx_n, mats = [], [], []
@@ -231,6 +234,10 @@ def fp64_sampled_error(db, per_matrix=4, seed=0):
         offC = torch.tensor([db.offC[mats[s]] + idx_m[s] + idx_n[s] * db.ldc[mats[s]]
                              for s in ss], device=dev)
         c = db.C[offC].double()
+        if C0 is not None and beta != 0.0:
+            c0 = beta * C0[offC].double()
+            exact = exact + c0
+            absb = absb + c0.abs()
         errs.append(((c - exact).abs() / absb.clamp_min(1e-300)).cpu())
     e = torch.cat(errs)
     return float(e.max()), float(e.mean()), S
@@ -409,7 +416,149 @@ def gpu_leg(args, rank, world, local):
                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                       "ms_per_step": round(ems, 3), "api": "bgemm_sgemm_vbatched (host copies "
                                                            "pinned)"}
+    if not args.no_stream:
+        out["stream"] = stream_leg(args, dev, s)
     return w, out
+
+
+# ------------------------------------------------------------ stream leg --
+def stream_leg(args, dev, s):
+    """The batch stream: successive batches (64..1024 matrices each, M, N, K
+    log-uniform in [1, 4096], U[-1, 1] entries, alpha = beta = 1).  One plan
+    per mode, created with the element-wise maximum of every batch's
+    requirements as capacity; its execute is captured once in a CUDA graph,
+    and each batch is uploaded with bgemm_plan_update (host planning of batch
+    b+1 overlaps the GPU running batch b) before one graph replay.  Reports
+    per-batch device latency (upload + kernels, CUDA events) p50/p99 and the
+    aggregate useful TFLOP/s over the whole stream."""
+    import types
+    import torch
+    import batchgemm_gb300 as bg
+    from batchgemm_gb300 import workloads
+
+    bs = workloads.stream_batches(0, args.stream_batches)
+    nb = len(bs)
+    al = lambda x: (x + 3) // 4 * 4  # 16-byte aligned starts
+    dims = {"A": lambda w: zip(w.M, w.K), "B": lambda w: zip(w.K, w.N),
+            "C": lambda w: zip(w.M, w.N)}
+    # operand pools twice the largest batch; matrices are laid out from a
+    # cursor that keeps moving (wrapping) across batches, so consecutive
+    # batches touch different memory and no batch reads the previous one's
+    # operands out of L2
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    pools, offs = {}, {}
+    for key in "ABC":
+        sizes = [[al(r * c) for r, c in dims[key](w)] for w in bs]
+        pool_n = 2 * max(sum(v) for v in sizes) + 64
+        cur, o_all = 0, []
+        for v in sizes:
+            o = []
+            for n in v:
+                if cur + n > pool_n:
+                    cur = 0
+                o.append(cur)
+                cur += n
+            o_all.append(o)
+        offs[key] = o_all
+        pools[key] = torch.empty(pool_n, dtype=torch.float32, device=dev).uniform_(
+            -1, 1, generator=g)
+    cap_batch = max(w.batch for w in bs)
+    ptr_host = torch.zeros((nb, 3, cap_batch), dtype=torch.int64, pin_memory=True)
+    for b, w in enumerate(bs):
+        for j, key in enumerate("ABC"):
+            base = pools[key].data_ptr()
+            ptr_host[b, j, :w.batch] = torch.tensor([base + 4 * o for o in offs[key][b]],
+                                                    dtype=torch.int64)
+    arrs = []
+    for w in bs:
+        lda = [max(1, m) for m in w.M]
+        ldb = [max(1, k) for k in w.K]
+        arrs.append(tuple(bg.int_array(v) for v in (w.M, w.N, w.K, lda, ldb, lda)))
+    flops = [w.flops() for w in bs]
+
+    def run(mode):
+        opts = {"kernel_family": "pair"} if mode in ("tf32x3", "bf16x3") else {}
+        t0 = time.perf_counter()
+        reqs = [bg.plan_requirements(*arrs[b], mode=mode, **opts) for b in range(nb)]
+        req_ms = (time.perf_counter() - t0) * 1e3 / nb
+        cap = bg.max_requirements(reqs)
+        ptr_dev = torch.zeros((3, cap_batch), dtype=torch.int64, device=dev)
+        pA, pB, pC = (ptr_dev[j].data_ptr() for j in range(3))
+        with torch.cuda.stream(s):
+            plan = bg.Plan(*arrs[0], mode=mode, stream=s, capacity=cap, **opts)
+            for b in range(3):  # warm-up outside the graph
+                ptr_dev.copy_(ptr_host[b], non_blocking=True)
+                plan.update(*arrs[b], stream=s)
+                plan.execute(1.0, pA, pB, 1.0, pC, stream=s)
+        s.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=s):
+            plan.execute(1.0, pA, pB, 1.0, pC, stream=s)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(nb)]
+        host_ms = []
+        torch.cuda.synchronize(dev)
+        with torch.cuda.stream(s):
+            for b in range(nb):
+                evs[b][0].record(s)
+                ptr_dev.copy_(ptr_host[b], non_blocking=True)
+                t0 = time.perf_counter()
+                plan.update(*arrs[b], stream=s)
+                host_ms.append((time.perf_counter() - t0) * 1e3)
+                graph.replay()
+                evs[b][1].record(s)
+        s.synchronize()
+        plan.check_device(stream=s)
+        lat = sorted(a.elapsed_time(c) for a, c in evs)
+        total_ms = evs[0][0].elapsed_time(evs[-1][1])
+        # accuracy of the last batch, run again from a snapshot of C
+        b = nb - 1
+        w = bs[b]
+        C0 = pools["C"].clone()
+        with torch.cuda.stream(s):
+            ptr_dev.copy_(ptr_host[b], non_blocking=True)
+            plan.update(*arrs[b], stream=s)
+            graph.replay()
+        s.synchronize()
+        view = types.SimpleNamespace(
+            batch=w.batch, M=w.M, N=w.N, K=w.K, lda=[max(1, m) for m in w.M],
+            ldb=[max(1, k) for k in w.K], ldc=[max(1, m) for m in w.M], offA=offs["A"][b],
+            offB=offs["B"][b], offC=offs["C"][b], A=pools["A"], B=pools["B"], C=pools["C"])
+        e_max, e_mean, n_s = fp64_sampled_error(view, per_matrix=2, C0=C0, beta=1.0)
+        del C0, graph
+        info = plan.info()
+        plan.close()
+        pct = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]
+        return {"tflops": round(sum(flops) / (total_ms * 1e-3) / 1e12, 3),
+                "total_ms": round(total_ms, 2),
+                "latency_ms_p50": round(pct(0.50), 4), "latency_ms_p99": round(pct(0.99), 4),
+                "latency_ms_max": round(lat[-1], 4),
+                "host_update_ms_p50": round(statistics.median(host_ms), 4),
+                "host_requirements_ms_mean": round(req_ms, 4),
+                "kernels_per_batch": info["kernels_per_execute"] + (0 if mode == "simt" else 1),
+                "capacity": cap,
+                "err_vs_fp64_last_batch": {"max": e_max, "mean": e_mean, "samples": n_s}}
+
+    out = {"workload": "stream_%d: %d successive batches, U{64..1024} matrices each, M, N, K "
+                       "log-uniform in [1, 4096], U[-1,1], alpha = beta = 1" % (nb, nb),
+           "useful_tflop_total": round(sum(flops) / 1e12, 3),
+           "per_batch_gflop_p50": round(statistics.median(flops) / 1e9, 2),
+           "timing": "per batch: CUDA events around pointer upload + bgemm_plan_update + "
+                     "graph replay on the launching stream; aggregate = all batches / first "
+                     "start to last stop; operands rotate through pools twice the largest "
+                     "batch (no L2 reuse between batches)"}
+    for mode in (args.mode, "simt") if args.mode != "simt" else ("simt",):
+        try:
+            out[mode] = run(mode)
+        except bg.BgemmError as e:
+            out[mode] = {"unavailable": e.message}
+    if args.mode != "simt" and "tflops" in out.get(args.mode, {}) and \
+            "tflops" in out.get("simt", {}):
+        out["ratio_vs_simt"] = round(out[args.mode]["tflops"] / out["simt"]["tflops"], 3)
+    for key in list(pools):
+        del pools[key]
+    return out
 
 
 def main():
@@ -474,6 +623,8 @@ def main():
     }
     if "e2e" in out:
         line["e2e"] = out["e2e"]
+    if "stream" in out:
+        line["stream"] = out["stream"]
     print(json.dumps(line), flush=True)
 
 

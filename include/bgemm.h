@@ -85,6 +85,18 @@ typedef struct bgemm_plan_info {
   int reserved[7];
 } bgemm_plan_info_t;
 
+/* Device sizes a batch needs inside a plan; bgemm_plan_requirements computes
+ * them, and bgemm_plan_options_t.capacity reserves them so that the plan can
+ * later take other batches through bgemm_plan_update. */
+typedef struct bgemm_plan_requirements {
+  int batch;               /* matrices                                       */
+  int tiles;               /* work items of the largest-first tile queue     */
+  int pack_jobs;           /* split/pack pre-pass jobs (tensor-core modes)   */
+  int kernel_family;       /* 0 SIMT, 1 one-SM tcgen05 tiles, 2 CTA-pair tiles */
+  size_t workspace_bytes;  /* split-operand workspace (tensor-core modes)    */
+  int reserved[4];
+} bgemm_plan_requirements_t;
+
 /* Options for bgemm_plan_create_ex (zero-initialise, then set fields). */
 typedef struct bgemm_plan_options {
   int force_tile_config;    /* -1: heuristic; otherwise a config id of the mode */
@@ -98,7 +110,13 @@ typedef struct bgemm_plan_options {
                                pre-pass.  Fewer HBM/L2 bytes, but on GB300 the
                                extra shared-memory traffic makes it slower, so
                                it is off by default (kept for comparison). */
-  int reserved[6];
+  int kernel_family;        /* split tensor-core modes: 0 chosen by the cost
+                               model, 1 one-SM tiles, 2 CTA-pair tiles        */
+  int reserved[5];
+  /* Capacity for bgemm_plan_update: each field is raised to the creating
+   * batch's own requirement, so all-zero means "this batch only".
+   * kernel_family is ignored here (see the field above). */
+  bgemm_plan_requirements_t capacity;
 } bgemm_plan_options_t;
 
 /* --- one-shot entry (host size arrays, like CUDA/framework/gemm.cu:39-41) ---
@@ -131,6 +149,45 @@ bgemm_status_t bgemm_plan_execute(bgemm_plan_t plan, float alpha,
                                   const float* const* dB, float beta,
                                   float* const* dC, bgemm_stream_t stream);
 bgemm_status_t bgemm_plan_info(bgemm_plan_t plan, bgemm_plan_info_t* info);
+
+/* --- batch streams: re-plan into an existing plan ------------------------
+ * No counterpart in the reference, whose driver plans, uploads and launches
+ * one batch per process run (CUDA/framework/gemm.cu:31-209).
+ *
+ * bgemm_plan_requirements: host-only planning of a batch (the same tile
+ * choice, queue and pre-pass layout as bgemm_plan_create_ex with these
+ * options) that reports the device sizes it needs; nothing is allocated and
+ * no GPU work is issued.  The element-wise maximum over the batches of a
+ * stream, passed as options->capacity, sizes a plan that can take each of
+ * them.
+ *
+ * bgemm_plan_update: plans a new batch (same mode, kernel family and
+ * options as at creation) into the plan's existing device buffers and
+ * uploads its descriptors, tile queue, pre-pass jobs and tensor maps on
+ * `stream`.  Device addresses, kernels and launch shapes stay the same, so a
+ * CUDA graph that captured bgemm_plan_execute stays valid and computes the
+ * new batch on its next launch (A/B/C pointer arrays are the caller's: put
+ * the new batch's pointers where the graph reads them).  The update is
+ * stream-ordered: executes enqueued on `stream` before it see the previous
+ * batch, later ones the new batch; work on other streams must be ordered by
+ * the caller.  Host staging is double-buffered, so the call blocks only
+ * until the upload of the update before the previous one has been consumed;
+ * it must not be called while `stream` is capturing.  A batch beyond the
+ * plan's capacity fails with BGEMM_ERROR_NOT_SUPPORTED and leaves the plan
+ * holding its previous batch. */
+bgemm_status_t bgemm_plan_requirements(const int* M, const int* N, const int* K,
+                                       const int* lda, const int* ldb,
+                                       const int* ldc, int batch,
+                                       bgemm_mode_t mode,
+                                       const bgemm_plan_options_t* options,
+                                       bgemm_plan_requirements_t* out);
+bgemm_status_t bgemm_plan_update(bgemm_plan_t plan, const int* M, const int* N,
+                                 const int* K, const int* lda, const int* ldb,
+                                 const int* ldc, int batch,
+                                 bgemm_stream_t stream);
+/* Capacity the plan was created with (what bgemm_plan_update accepts). */
+bgemm_status_t bgemm_plan_capacity(bgemm_plan_t plan,
+                                   bgemm_plan_requirements_t* out);
 /* Profiling hook (no counterpart in the reference, which brackets its whole
  * launch loop with events, CUDA/framework/gemm.cu:203-214): every following
  * bgemm_plan_execute records ev_start / ev_stop (cudaEvent_t; either may be

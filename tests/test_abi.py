@@ -169,3 +169,36 @@ def test_reference_dataset_planned(built_lib):
         M, N, K = shapes[:b, 0].tolist(), shapes[:b, 1].tolist(), shapes[:b, 2].tolist()
         cfgs, items = simt_queue(M, N, K)
         coverage_ok(M, N, cfgs, items)
+
+
+def test_option_structs_match_the_header(tmp_path):
+    """ctypes mirrors of the option / requirement / info structs have the C
+    header's sizes and field offsets (gcc compiles a probe of the header)."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        pytest.skip("no gcc")
+    structs = {"bgemm_plan_options_t": bg.PlanOptions,
+               "bgemm_plan_requirements_t": bg.PlanRequirements,
+               "bgemm_plan_info_t": bg.PlanInfo}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "bgemm.h"', 'int main(void){']
+    for cname, py in structs.items():
+        lines.append('printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f in py._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f[0], cname,
+                                                                          f[0]))
+    lines.append("return 0;}")
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "probe"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    out = subprocess.check_output([str(exe)]).decode().split("\n")
+    got = {}
+    for line in out:
+        if line:
+            c, f, v = line.split()
+            got[(c, f)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "sizeof")] == ctypes.sizeof(py), cname
+        for f in py._fields_:
+            assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])
