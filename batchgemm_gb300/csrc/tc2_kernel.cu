@@ -10,8 +10,8 @@
 // the L2 traffic per flop of the one-SM kernel (tc_kernel.cu), which is what
 // bounds that kernel.
 //
-// Accumulation is group-promoted exactly as in tc_kernel.cu: each group (one
-// 128-byte K slice, or one MMA for K <= 64) accumulates into a fresh 256-column
+// Accumulation is group-promoted exactly as in tc_kernel.cu: each group (two
+// 128-byte K slices, or one MMA for K <= 64) accumulates into a fresh 256-column
 // TMEM buffer (2-deep ring) with the small products first, and the epilogue
 // warps of both CTAs add it into FP32 registers with round-to-nearest.
 //
@@ -46,6 +46,8 @@ constexpr int kEpiWarps2 = 8;              // 2 per TMEM lane quadrant
 constexpr int kCols = 128;                 // accumulator columns per epilogue warp
 constexpr int kThreads2 = 64 + kEpiWarps2 * 32;
 constexpr int kFineK2 = 64;
+// Matrices with K above kFineK2 promote every kGroupKB2 128-byte K slices.
+constexpr int kGroupKB2 = 2;
 
 __device__ __forceinline__ int snake(int c, int t, int ncl) {
   const int base = t * ncl;
@@ -212,22 +214,28 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
             }
             if (!ok) break;
           } else {
-            if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
-              ok = false;
-              break;
+            // a group spans kGroupKB2 slices; small products of each slice first
+            const bool first = (kb % kGroupKB2) == 0;
+            if (first) {
+              if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
+                ok = false;
+                break;
+              }
+              tc_fence_after();
             }
-            tc_fence_after();
             const uint32_t buf = tmem + acc.idx * 256u;
             for (int s = 0; s < s_end; ++s) {
               mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + 32u * s), idesc,
-                             s > 0 ? 1u : 0u);
+                             (first && s == 0) ? 0u : 1u);
               mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + kB + 32u * s), idesc,
                              1u);
             }
             for (int s = 0; s < s_end; ++s)
               mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
-            mma_commit_pair(tfull(acc.idx));
-            acc.next(kNAcc);
+            if ((kb % kGroupKB2) == kGroupKB2 - 1 || kb == nk - 1) {
+              mma_commit_pair(tfull(acc.idx));
+              acc.next(kNAcc);
+            }
           }
           mma_commit_pair(empty(st.idx));
           st.next(kS);
@@ -259,7 +267,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       if (beta != 0.0f) c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
       const int nk = (d.K + KE - 1) / KE;
       const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
-      const int ngroups = (d.K <= kFineK2) ? nsub : nk;
+      const int ngroups = (d.K <= kFineK2) ? nsub : (nk + kGroupKB2 - 1) / kGroupKB2;
       float r[kCols];
 #pragma unroll
       for (int j = 0; j < kCols; ++j) r[j] = 0.0f;
