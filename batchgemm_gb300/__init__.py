@@ -83,12 +83,30 @@ class PlanOptions(ctypes.Structure):
     _fields_ = [("force_tile_config", ctypes.c_int), ("max_ctas", ctypes.c_int),
                 ("disable_rebalance", ctypes.c_int), ("host_tensor_maps", ctypes.c_int),
                 ("split_in_kernel", ctypes.c_int), ("kernel_family", ctypes.c_int),
-                ("reserved", ctypes.c_int * 5), ("capacity", PlanRequirements)]
+                ("layout", ctypes.c_int), ("trans_a", ctypes.c_int), ("trans_b", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2), ("capacity", PlanRequirements)]
+
+
+LAYOUTS = {"col": 0, "row": 1}
+
+
+def _layout(v) -> int:
+    return LAYOUTS[v] if isinstance(v, str) else int(v)
+
+
+def _op(v) -> int:
+    if isinstance(v, str):
+        return {"N": 0, "T": 1, "n": 0, "t": 1}[v]
+    return int(bool(v))
 
 
 def _options(force_tile_config=-1, max_ctas=0, rebalance=True, host_tensor_maps=False,
-             split_in_kernel=False, kernel_family="auto", capacity=None) -> PlanOptions:
+             split_in_kernel=False, kernel_family="auto", capacity=None, layout="col",
+             trans_a=False, trans_b=False) -> PlanOptions:
     opt = PlanOptions()
+    opt.layout = _layout(layout)
+    opt.trans_a = _op(trans_a)
+    opt.trans_b = _op(trans_b)
     opt.force_tile_config = force_tile_config
     opt.max_ctas = max_ctas
     opt.disable_rebalance = 0 if rebalance else 1
@@ -120,6 +138,8 @@ def lib() -> ctypes.CDLL:
     i, f, vp = ctypes.c_int, ctypes.c_float, ctypes.c_void_p
     ip = ctypes.POINTER(ctypes.c_int)
     L.bgemm_sgemm_vbatched.argtypes = [ip, ip, ip, f, vp, ip, vp, ip, f, vp, ip, i, i, vp]
+    L.bgemm_sgemm_vbatched_ex.argtypes = [i, i, i, ip, ip, ip, f, vp, ip, vp, ip, f, vp, ip, i, i,
+                                          vp]
     L.bgemm_plan_create.argtypes = [ctypes.POINTER(vp), ip, ip, ip, ip, ip, ip, i, i, vp]
     L.bgemm_plan_create_ex.argtypes = [ctypes.POINTER(vp), ip, ip, ip, ip, ip, ip, i, i, vp,
                                        ctypes.POINTER(PlanOptions)]
@@ -148,7 +168,7 @@ def lib() -> ctypes.CDLL:
                  "bgemm_plan_destroy", "bgemm_framework_gemm", "bgemm_framework_check_device",
                  "bgemm_framework_gemm_noalloc", "bgemm_device_info",
                  "bgemm_plan_set_kernel_events", "bgemm_plan_requirements",
-                 "bgemm_plan_update", "bgemm_plan_capacity"):
+                 "bgemm_plan_update", "bgemm_plan_capacity", "bgemm_sgemm_vbatched_ex"):
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -215,17 +235,27 @@ def max_requirements(reqs) -> dict:
     return out
 
 
+def sgemm_vbatched_ex(layout, trans_a, trans_b, M, N, K, alpha, dA, lda, dB, ldb, beta, dC,
+                      ldc, mode="simt", stream=None) -> None:
+    """bgemm_sgemm_vbatched_ex: storage order ("col"/"row") and op(A), op(B) ("N"/"T")."""
+    _check(lib().bgemm_sgemm_vbatched_ex(_layout(layout), _op(trans_a), _op(trans_b), _iarr(M),
+                                         _iarr(N), _iarr(K), float(alpha), dA, _iarr(lda), dB,
+                                         _iarr(ldb), float(beta), dC, _iarr(ldc), len(M),
+                                         _mode(mode), _stream(stream)))
+
+
 class Plan:
     """bgemm_plan_create / execute / update / destroy."""
 
     def __init__(self, M, N, K, lda, ldb, ldc, mode="simt", stream=None,
                  force_tile_config: int = -1, max_ctas: int = 0, rebalance: bool = True,
                  host_tensor_maps: bool = False, split_in_kernel: bool = False,
-                 kernel_family="auto", capacity=None):
+                 kernel_family="auto", capacity=None, layout="col", trans_a=False,
+                 trans_b=False):
         self._h = ctypes.c_void_p()
         self.batch = len(M)
         opt = _options(force_tile_config, max_ctas, rebalance, host_tensor_maps,
-                       split_in_kernel, kernel_family, capacity)
+                       split_in_kernel, kernel_family, capacity, layout, trans_a, trans_b)
         _check(lib().bgemm_plan_create_ex(ctypes.byref(self._h), _iarr(M), _iarr(N), _iarr(K),
                                           _iarr(lda), _iarr(ldb), _iarr(ldc), len(M),
                                           _mode(mode), _stream(stream), ctypes.byref(opt)))

@@ -11,8 +11,12 @@ struct MatDesc {
   int M, N, K;
   int lda, ldb, ldc;
   int cfg;    // tile configuration id of the plan's mode
-  int aux;    // tensor-core modes: index of the matrix's packed operands; else 0
+  int aux;    // flag bits below (plan paths); size bin (device-built framework path)
 };
+// MatDesc::aux flags: op(A) = A^T (A stored K x M), op(B) = B^T (B stored
+// N x K); bit 30 is the tensor-core modes' operand swap.
+constexpr int kTransAFlag = 1 << 28;
+constexpr int kTransBFlag = 1 << 29;
 
 // One work item of the largest-first tile queue (8 bytes).
 struct TileItem {

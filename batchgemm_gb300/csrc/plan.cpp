@@ -174,7 +174,8 @@ bgemm_status_t choose_tiles(int ncfg, TileEval eval, const int* M, const int* N,
 static bgemm_status_t check_args(const int* M, const int* N, const int* K, const int* lda,
                                  const int* ldb, const int* ldc, int batch, int mode,
                                  int arg_M, int arg_N, int arg_K, int arg_lda, int arg_ldb,
-                                 int arg_ldc, int arg_batch, int arg_mode) {
+                                 int arg_ldc, int arg_batch, int arg_mode, bool row_major = false,
+                                 bool ta = false, bool tb = false) {
   if (batch < 0) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_batch, -1, "batch < 0");
   if (mode < BGEMM_MODE_SIMT_FP32 || mode > BGEMM_MODE_BF16X3)
     return set_error(BGEMM_ERROR_INVALID_VALUE, arg_mode, -1, "unknown mode %d", mode);
@@ -189,15 +190,21 @@ static bgemm_status_t check_args(const int* M, const int* N, const int* K, const
     if (M[i] < 0) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_M, i, "M[%d] = %d < 0", i, M[i]);
     if (N[i] < 0) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_N, i, "N[%d] = %d < 0", i, N[i]);
     if (K[i] < 0) return set_error(BGEMM_ERROR_INVALID_VALUE, arg_K, i, "K[%d] = %d < 0", i, K[i]);
-    if (lda[i] < std::max(1, M[i]))
-      return set_error(BGEMM_ERROR_INVALID_VALUE, arg_lda, i, "lda[%d] = %d < max(1, M = %d)", i,
-                       lda[i], M[i]);
-    if (ldb[i] < std::max(1, K[i]))
-      return set_error(BGEMM_ERROR_INVALID_VALUE, arg_ldb, i, "ldb[%d] = %d < max(1, K = %d)", i,
-                       ldb[i], K[i]);
-    if (ldc[i] < std::max(1, M[i]))
-      return set_error(BGEMM_ERROR_INVALID_VALUE, arg_ldc, i, "ldc[%d] = %d < max(1, M = %d)", i,
-                       ldc[i], M[i]);
+    // the extent each leading dimension spans (rows of a column-major
+    // matrix, columns of a row-major one)
+    const char* na = row_major ? (ta ? "M" : "K") : (ta ? "K" : "M");
+    const char* nb = row_major ? (tb ? "K" : "N") : (tb ? "N" : "K");
+    const char* nc = row_major ? "N" : "M";
+    auto dim = [&](const char* n) { return n[0] == 'M' ? M[i] : n[0] == 'N' ? N[i] : K[i]; };
+    if (lda[i] < std::max(1, dim(na)))
+      return set_error(BGEMM_ERROR_INVALID_VALUE, arg_lda, i, "lda[%d] = %d < max(1, %s = %d)", i,
+                       lda[i], na, dim(na));
+    if (ldb[i] < std::max(1, dim(nb)))
+      return set_error(BGEMM_ERROR_INVALID_VALUE, arg_ldb, i, "ldb[%d] = %d < max(1, %s = %d)", i,
+                       ldb[i], nb, dim(nb));
+    if (ldc[i] < std::max(1, dim(nc)))
+      return set_error(BGEMM_ERROR_INVALID_VALUE, arg_ldc, i, "ldc[%d] = %d < max(1, %s = %d)", i,
+                       ldc[i], nc, dim(nc));
   }
   return BGEMM_SUCCESS;
 }
@@ -308,7 +315,8 @@ static bgemm_status_t plan_batch(bgemm_plan_s* p, const int* M, const int* N, co
   std::memset(bp.hist, 0, sizeof(bp.hist));
   bp.flops = bp.bytes = 0;
   for (int i = 0; i < batch; ++i) {
-    bp.descs[i] = MatDesc{M[i], N[i], K[i], lda[i], ldb[i], ldc[i], mp[i].cfg < 0 ? 0 : mp[i].cfg, 0};
+    bp.descs[i] = MatDesc{M[i], N[i], K[i], lda[i], ldb[i], ldc[i], mp[i].cfg < 0 ? 0 : mp[i].cfg,
+                          p->aux_trans};
     bp.flops += 2.0 * M[i] * (double)N[i] * K[i];
     bp.bytes += 4.0 * ((double)M[i] * K[i] + (double)K[i] * N[i] + (double)M[i] * N[i]);
     if (mp[i].cfg >= 0 && mp[i].cfg < 16) bp.hist[mp[i].cfg]++;
@@ -428,12 +436,41 @@ static bgemm_status_t stream_not_capturing(cudaStream_t stream, int arg) {
   return BGEMM_SUCCESS;
 }
 
+// Storage order and transposition of the options -> the planned column-major
+// product.  Row-major plans compute C^T = op(B)^T op(A)^T: the B array is the
+// planned A side (with B's flag) and the A array the planned B side.
+static bgemm_status_t set_orientation(bgemm_plan_s* p, int arg) {
+  const bgemm_plan_options_t& o = p->opt;
+  if ((o.layout != 0 && o.layout != 1) || (o.trans_a != 0 && o.trans_a != 1) ||
+      (o.trans_b != 0 && o.trans_b != 1))
+    return set_error(BGEMM_ERROR_INVALID_VALUE, arg, -1,
+                     "layout, trans_a and trans_b must each be 0 or 1");
+  p->row_major = o.layout == BGEMM_ROW_MAJOR;
+  const bool pa = p->row_major ? o.trans_b : o.trans_a;
+  const bool pb = p->row_major ? o.trans_a : o.trans_b;
+  p->aux_trans = (pa ? kTransAFlag : 0) | (pb ? kTransBFlag : 0);
+  return BGEMM_SUCCESS;
+}
+
+// plan_batch on the planned product's shapes (row-major: swapped operands).
+static bgemm_status_t plan_batch_oriented(bgemm_plan_s* p, const int* M, const int* N,
+                                          const int* K, const int* lda, const int* ldb,
+                                          const int* ldc, int batch, bool first, BatchPlan& bp) {
+  if (p->row_major) return plan_batch(p, N, M, K, ldb, lda, ldc, batch, first, bp);
+  return plan_batch(p, M, N, K, lda, ldb, ldc, batch, first, bp);
+}
+
 bgemm_status_t plan_create(bgemm_plan_t* out, const int* M, const int* N, const int* K,
                            const int* lda, const int* ldb, const int* ldc, int batch, int mode,
                            cudaStream_t stream, const bgemm_plan_options_t* opt) {
   if (!out) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
   *out = nullptr;
-  bgemm_status_t st = check_args(M, N, K, lda, ldb, ldc, batch, mode, 2, 3, 4, 5, 6, 7, 8, 9);
+  bgemm_plan_s probe;
+  probe.opt = opt ? *opt : default_options();
+  bgemm_status_t st = set_orientation(&probe, 11);
+  if (st != BGEMM_SUCCESS) return st;
+  st = check_args(M, N, K, lda, ldb, ldc, batch, mode, 2, 3, 4, 5, 6, 7, 8, 9, probe.row_major,
+                  probe.opt.trans_a != 0, probe.opt.trans_b != 0);
   if (st != BGEMM_SUCCESS) return st;
   if (opt && (st = check_capacity_option(opt->capacity)) != BGEMM_SUCCESS) return st;
   DeviceFacts df;
@@ -443,11 +480,13 @@ bgemm_status_t plan_create(bgemm_plan_t* out, const int* M, const int* N, const 
   auto* p = new bgemm_plan_s();
   p->mode = mode;
   p->facts = df;
-  p->opt = opt ? *opt : default_options();
+  p->opt = probe.opt;
+  p->row_major = probe.row_major;
+  p->aux_trans = probe.aux_trans;
   p->info.mode = mode;
   BatchPlan bp;
   if (mode != BGEMM_MODE_SIMT_FP32) st = tc_init(p, &p->opt);
-  if (st == BGEMM_SUCCESS) st = plan_batch(p, M, N, K, lda, ldb, ldc, batch, true, bp);
+  if (st == BGEMM_SUCCESS) st = plan_batch_oriented(p, M, N, K, lda, ldb, ldc, batch, true, bp);
   if (st == BGEMM_SUCCESS) {
     const bgemm_plan_requirements_t& c = p->opt.capacity;
     p->cap = bp.req;
@@ -472,7 +511,8 @@ bgemm_status_t plan_update(bgemm_plan_t p, const int* M, const int* N, const int
                            cudaStream_t stream) {
   if (!p) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
   bgemm_status_t st =
-      check_args(M, N, K, lda, ldb, ldc, batch, p->mode, 2, 3, 4, 5, 6, 7, 8, 8);
+      check_args(M, N, K, lda, ldb, ldc, batch, p->mode, 2, 3, 4, 5, 6, 7, 8, 8, p->row_major,
+                 p->opt.trans_a != 0, p->opt.trans_b != 0);
   if (st != BGEMM_SUCCESS) return st;
   int dev = -1;
   cudaGetDevice(&dev);
@@ -488,7 +528,7 @@ bgemm_status_t plan_update(bgemm_plan_t p, const int* M, const int* N, const int
     return set_error(BGEMM_ERROR_NOT_SUPPORTED, 8, -1, "batch %d exceeds the plan's capacity %d",
                      batch, p->cap.batch);
   BatchPlan bp;
-  st = plan_batch(p, M, N, K, lda, ldb, ldc, batch, false, bp);
+  st = plan_batch_oriented(p, M, N, K, lda, ldb, ldc, batch, false, bp);
   if (st != BGEMM_SUCCESS) return st;
   const bgemm_plan_requirements_t& r = bp.req;
   if (r.tiles > p->cap.tiles || r.pack_jobs > p->cap.pack_jobs ||
@@ -505,19 +545,22 @@ bgemm_status_t plan_requirements(const int* M, const int* N, const int* K, const
                                  const int* ldb, const int* ldc, int batch, int mode,
                                  const bgemm_plan_options_t* opt,
                                  bgemm_plan_requirements_t* out) {
-  bgemm_status_t st = check_args(M, N, K, lda, ldb, ldc, batch, mode, 1, 2, 3, 4, 5, 6, 7, 8);
+  bgemm_plan_s p;
+  p.opt = opt ? *opt : default_options();
+  bgemm_status_t st = set_orientation(&p, 9);
+  if (st != BGEMM_SUCCESS) return st;
+  st = check_args(M, N, K, lda, ldb, ldc, batch, mode, 1, 2, 3, 4, 5, 6, 7, 8, p.row_major,
+                  p.opt.trans_a != 0, p.opt.trans_b != 0);
   if (st != BGEMM_SUCCESS) return st;
   if (!out) return set_error(BGEMM_ERROR_INVALID_VALUE, 10, -1, "out is NULL");
   DeviceFacts df;
   st = device_facts(&df);
   if (st != BGEMM_SUCCESS) return st;
-  bgemm_plan_s p;
   p.mode = mode;
   p.facts = df;
-  p.opt = opt ? *opt : default_options();
   BatchPlan bp;
   if (mode != BGEMM_MODE_SIMT_FP32) st = tc_init(&p, &p.opt);
-  if (st == BGEMM_SUCCESS) st = plan_batch(&p, M, N, K, lda, ldb, ldc, batch, true, bp);
+  if (st == BGEMM_SUCCESS) st = plan_batch_oriented(&p, M, N, K, lda, ldb, ldc, batch, true, bp);
   if (p.tc) tc_plan_release(&p);
   if (st == BGEMM_SUCCESS) *out = bp.req;
   return st;
@@ -531,6 +574,7 @@ bgemm_status_t plan_execute(bgemm_plan_t p, float alpha, const float* const* dA,
   if (!dA) return set_error(BGEMM_ERROR_INVALID_VALUE, 3, -1, "dA is NULL");
   if (!dB) return set_error(BGEMM_ERROR_INVALID_VALUE, 4, -1, "dB is NULL");
   if (!dC) return set_error(BGEMM_ERROR_INVALID_VALUE, 6, -1, "dC is NULL");
+  if (p->row_major) std::swap(dA, dB);
   if (p->mode == BGEMM_MODE_SIMT_FP32) {
     SimtParams sp{p->d_descs, p->d_items,  p->n_items, p->d_counters + kHdrItems,
                   p->d_counters, alpha,    beta,       dA, dB, dC};
@@ -570,13 +614,13 @@ PlanCache& cache() {
 
 bgemm_status_t cached_plan(bgemm_plan_t* out, const int* M, const int* N, const int* K,
                            const int* lda, const int* ldb, const int* ldc, int batch, int mode,
-                           cudaStream_t stream) {
+                           cudaStream_t stream, int layout = 0, int ta = 0, int tb = 0) {
   int dev = 0;
   cudaGetDevice(&dev);
   std::string key;
-  key.resize(sizeof(int) * (3 + 6 * (size_t)batch) + sizeof(void*));
+  key.resize(sizeof(int) * (4 + 6 * (size_t)batch) + sizeof(void*));
   char* k = &key[0];
-  int hdr[3] = {dev, mode, batch};
+  int hdr[4] = {dev, mode, batch, layout | (ta << 1) | (tb << 2)};
   std::memcpy(k, hdr, sizeof(hdr));
   k += sizeof(hdr);
   void* sp = stream;
@@ -595,7 +639,11 @@ bgemm_status_t cached_plan(bgemm_plan_t* out, const int* M, const int* N, const 
     return BGEMM_SUCCESS;
   }
   bgemm_plan_t p = nullptr;
-  bgemm_status_t st = plan_create(&p, M, N, K, lda, ldb, ldc, batch, mode, stream, nullptr);
+  bgemm_plan_options_t opt = default_options();
+  opt.layout = layout;
+  opt.trans_a = ta;
+  opt.trans_b = tb;
+  bgemm_status_t st = plan_create(&p, M, N, K, lda, ldb, ldc, batch, mode, stream, &opt);
   if (st != BGEMM_SUCCESS) return st;
   if (c.map.size() >= PlanCache::kMax) {
     const std::string& victim = c.lru.back();
@@ -619,32 +667,67 @@ using namespace bgemm;
 
 extern "C" {
 
+}  // extern "C"
+
+namespace bgemm {
+// Shared body of the one-shot entries; arg[] holds the caller's argument
+// numbers of M, N, K, dA, lda, dB, ldb, dC, ldc, batch, mode.
+static bgemm_status_t vbatched(int layout, int ta, int tb, const int* M, const int* N,
+                               const int* K, float alpha, const float* const* dA, const int* lda,
+                               const float* const* dB, const int* ldb, float beta,
+                               float* const* dC, const int* ldc, int batch, int mode,
+                               cudaStream_t stream, const int (&arg)[11]) {
+  bgemm_status_t st = check_args(M, N, K, lda, ldb, ldc, batch, mode, arg[0], arg[1], arg[2],
+                                 arg[4], arg[6], arg[8], arg[9], arg[10], layout == 1, ta, tb);
+  if (st != BGEMM_SUCCESS || batch == 0) return st;
+  bool any = false;
+  for (int i = 0; i < batch && !any; ++i) any = M[i] > 0 && N[i] > 0;
+  if (!any) return BGEMM_SUCCESS;
+  if (!dA) return set_error(BGEMM_ERROR_INVALID_VALUE, arg[3], -1, "dA is NULL");
+  if (!dB) return set_error(BGEMM_ERROR_INVALID_VALUE, arg[5], -1, "dB is NULL");
+  if (!dC) return set_error(BGEMM_ERROR_INVALID_VALUE, arg[7], -1, "dC is NULL");
+  bgemm_plan_t p = nullptr;
+  st = cached_plan(&p, M, N, K, lda, ldb, ldc, batch, mode, stream, layout, ta, tb);
+  if (st != BGEMM_SUCCESS) return st;
+  st = plan_execute(p, alpha, dA, dB, beta, dC, stream);
+  if (st == BGEMM_ERROR_INVALID_VALUE && t_err_arg > 0) {
+    // plan_execute numbers its own arguments; map them to this entry point
+    const int map[7] = {0, 0, 0, arg[3], arg[5], 0, arg[7]};
+    if (t_err_arg < 7 && map[t_err_arg]) t_err_arg = map[t_err_arg];
+  }
+  return st;
+}
+}  // namespace bgemm
+
+extern "C" {
+
 bgemm_status_t bgemm_sgemm_vbatched(const int* M, const int* N, const int* K, float alpha,
                                     const float* const* dA, const int* lda,
                                     const float* const* dB, const int* ldb, float beta,
                                     float* const* dC, const int* ldc, int batch,
                                     bgemm_mode_t mode, bgemm_stream_t stream) {
   clear_error();
-  bgemm_status_t st =
-      check_args(M, N, K, lda, ldb, ldc, batch, (int)mode, 1, 2, 3, 6, 8, 11, 12, 13);
-  if (st != BGEMM_SUCCESS || batch == 0) return st;
-  bool any = false;
-  for (int i = 0; i < batch && !any; ++i) any = M[i] > 0 && N[i] > 0;
-  if (!any) return BGEMM_SUCCESS;
-  if (!dA) return set_error(BGEMM_ERROR_INVALID_VALUE, 5, -1, "dA is NULL");
-  if (!dB) return set_error(BGEMM_ERROR_INVALID_VALUE, 7, -1, "dB is NULL");
-  if (!dC) return set_error(BGEMM_ERROR_INVALID_VALUE, 10, -1, "dC is NULL");
-  bgemm_plan_t p = nullptr;
-  st = cached_plan(&p, M, N, K, lda, ldb, ldc, batch, (int)mode, stream);
-  if (st != BGEMM_SUCCESS) return st;
-  st = plan_execute(p, alpha, dA, dB, beta, dC, stream);
-  if (st != BGEMM_SUCCESS && t_err_arg == 0) return st;
-  // plan_execute numbers its own arguments; map them to this entry point
-  if (st == BGEMM_ERROR_INVALID_VALUE) {
-    const int map[7] = {0, 0, 0, 5, 7, 0, 10};
-    if (t_err_arg >= 0 && t_err_arg < 7 && map[t_err_arg]) t_err_arg = map[t_err_arg];
-  }
-  return st;
+  static const int arg[11] = {1, 2, 3, 5, 6, 7, 8, 10, 11, 12, 13};
+  return vbatched(0, 0, 0, M, N, K, alpha, dA, lda, dB, ldb, beta, dC, ldc, batch, (int)mode,
+                  stream, arg);
+}
+
+bgemm_status_t bgemm_sgemm_vbatched_ex(bgemm_layout_t layout, bgemm_op_t transA,
+                                       bgemm_op_t transB, const int* M, const int* N,
+                                       const int* K, float alpha, const float* const* dA,
+                                       const int* lda, const float* const* dB, const int* ldb,
+                                       float beta, float* const* dC, const int* ldc, int batch,
+                                       bgemm_mode_t mode, bgemm_stream_t stream) {
+  clear_error();
+  if (layout != BGEMM_COL_MAJOR && layout != BGEMM_ROW_MAJOR)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "unknown layout %d", (int)layout);
+  if (transA != BGEMM_OP_N && transA != BGEMM_OP_T)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 2, -1, "unknown transA %d", (int)transA);
+  if (transB != BGEMM_OP_N && transB != BGEMM_OP_T)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 3, -1, "unknown transB %d", (int)transB);
+  static const int arg[11] = {4, 5, 6, 8, 9, 10, 11, 13, 14, 15, 16};
+  return vbatched((int)layout, (int)transA, (int)transB, M, N, K, alpha, dA, lda, dB, ldb, beta,
+                  dC, ldc, batch, (int)mode, stream, arg);
 }
 
 bgemm_status_t bgemm_plan_create(bgemm_plan_t* plan, const int* M, const int* N, const int* K,

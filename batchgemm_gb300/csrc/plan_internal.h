@@ -59,6 +59,11 @@ struct bgemm_plan_s {
   bgemm::DeviceFacts facts{};
   bgemm_plan_options_t opt{};      // options of creation, reused by updates
   bgemm_plan_requirements_t cap{}; // capacity of the device buffers
+  // Row-major plans run the column-major product C^T = op(B)^T op(A)^T:
+  // their shapes are planned as (N, M, K, ldb, lda, ldc) with the trans flags
+  // of B and A, and execute passes dB as A and dA as B.
+  bool row_major = false;
+  int aux_trans = 0;               // kTransAFlag / kTransBFlag of the planned product
   void* d_mem = nullptr;           // header | descs[cap] | items[cap]
   void* h_stage[2] = {nullptr, nullptr};  // double-buffered pinned staging, same layout
   cudaEvent_t ev_stage[2] = {nullptr, nullptr};  // upload from h_stage[i] consumed

@@ -9,11 +9,13 @@
 //
 // Each item is one BM x BN output tile of one matrix.  256 threads form a
 // 16 x 16 grid; each owns a TM x TN register tile.  Operands stream through a
-// 4-stage cp.async ring of BK = 8 k-slices:
-//   A slice: [k][BM]     (column of A, 16-byte cp.async when lda % 4 == 0 and
-//                         A is 16-byte aligned, 4-byte otherwise)
-//   B slice: [k][BN + 4] (transposed on the way in by 4-byte cp.async; the
-//                         +4 pad keeps the scattered writes conflict-free)
+// 4-stage cp.async ring of BK = 8 k-slices, [k][BM + 4] for op(A) and
+// [k][BN + 4] for op(B).  An operand whose rows of the slice are contiguous
+// in memory (A column-major, or B stored transposed) is copied with 16-byte
+// cp.async when its leading dimension and base allow it, else 4-byte; an
+// operand contiguous along k (B column-major, or A stored transposed) is
+// transposed on the way in by 4-byte cp.async (the +4 pad keeps the
+// scattered shared-memory writes conflict-free).
 // Edges are zero-filled by the cp.async source size, so any M, N, K >= 0 and
 // any leading dimension work.  Every output element is a single fma chain
 // over k in order (bit-exact with the reference's tile bodies and with the
@@ -31,7 +33,7 @@ constexpr int kThreads = 256;
 constexpr int kBK = 8;
 constexpr int kStages = 4;
 constexpr int kPadB = 4;
-constexpr int kMaxStageFloats = kBK * (128 + 128 + kPadB);
+constexpr int kMaxStageFloats = kBK * (128 + kPadB + 128 + kPadB);
 constexpr int kSmemBytes = kStages * kMaxStageFloats * 4;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -76,6 +78,58 @@ struct VecLd<4> {
   }
 };
 
+// Slice k0 .. k0+kBK-1 of R operand rows r0 .. r0+R-1 into s[k][LDS] when
+// element (r, k) sits at X[r + k*ldx] (rows contiguous).  Out-of-range
+// elements are zero-filled through the cp.async source size.
+template <int R, int LDS>
+__device__ __forceinline__ void load_rows_contig(const float* X, long long ldx, int rows, int r0,
+                                                 int k0, int K, float* s, bool vec, int tid) {
+  if (vec) {
+    constexpr int CH = R * kBK / 4;
+#pragma unroll
+    for (int c0 = 0; c0 < CH; c0 += kThreads) {
+      const int c = c0 + tid;
+      if (CH % kThreads == 0 || c < CH) {
+        const int rr = (c % (R / 4)) * 4, kk = c / (R / 4);
+        const int gr = r0 + rr, gk = k0 + kk;
+        const int valid = (gk < K) ? min(max(rows - gr, 0), 4) : 0;
+        const float* src = valid ? X + gk * ldx + gr : X;
+        cp_async16(smem_u32(s + kk * LDS + rr), src, valid * 4);
+      }
+    }
+  } else {
+    constexpr int EL = R * kBK;
+#pragma unroll
+    for (int e0 = 0; e0 < EL; e0 += kThreads) {
+      const int e = e0 + tid;
+      if (EL % kThreads == 0 || e < EL) {
+        const int rr = e % R, kk = e / R;
+        const int gr = r0 + rr, gk = k0 + kk;
+        const bool v = (gk < K) && (gr < rows);
+        cp_async4(smem_u32(s + kk * LDS + rr), v ? X + gk * ldx + gr : X, v ? 4 : 0);
+      }
+    }
+  }
+}
+
+// The same slice when element (r, k) sits at X[k + r*ldx] (k contiguous):
+// consecutive threads walk k, so global reads stay in runs of kBK floats.
+template <int R, int LDS>
+__device__ __forceinline__ void load_k_contig(const float* X, long long ldx, int rows, int r0,
+                                              int k0, int K, float* s, int tid) {
+  constexpr int EL = R * kBK;
+#pragma unroll
+  for (int e0 = 0; e0 < EL; e0 += kThreads) {
+    const int e = e0 + tid;
+    if (EL % kThreads == 0 || e < EL) {
+      const int kk = e % kBK, rr = e / kBK;
+      const int gk = k0 + kk, gr = r0 + rr;
+      const bool v = (gk < K) && (gr < rows);
+      cp_async4(smem_u32(s + kk * LDS + rr), v ? X + gr * ldx + gk : X, v ? 4 : 0);
+    }
+  }
+}
+
 template <int BM, int BN, int TM, int TN>
 __device__ __forceinline__ void simt_tile(const MatDesc& d, int tm, int tn,
                                           const float* __restrict__ A,
@@ -88,8 +142,9 @@ __device__ __forceinline__ void simt_tile(const MatDesc& d, int tm, int tn,
   constexpr int TNH = TN > 4 ? 4 : TN;
   constexpr int HM = TM / TMH;          // halves along m (2 for TM = 8)
   constexpr int HN = TN / TNH;
+  constexpr int LDAS = BM + kPadB;
   constexpr int LDBS = BN + kPadB;
-  constexpr int A_STAGE = kBK * BM;
+  constexpr int A_STAGE = kBK * LDAS;
   constexpr int STAGE = A_STAGE + kBK * LDBS;
 
   const int tid = threadIdx.x;
@@ -119,49 +174,22 @@ __device__ __forceinline__ void simt_tile(const MatDesc& d, int tm, int tn,
     }
 
   const int nkb = (K + kBK - 1) / kBK;
-  const bool a_vec = ((reinterpret_cast<uintptr_t>(A) & 15u) == 0) && ((d.lda & 3) == 0);
+  const bool ta = (d.aux & kTransAFlag) != 0, tb = (d.aux & kTransBFlag) != 0;
+  const bool a_vec = !ta && ((reinterpret_cast<uintptr_t>(A) & 15u) == 0) && ((d.lda & 3) == 0);
+  const bool b_vec = tb && ((reinterpret_cast<uintptr_t>(B) & 15u) == 0) && ((d.ldb & 3) == 0);
 
   auto load_stage = [&](int kb, int slot) {
     float* sA = smem + slot * STAGE;
     float* sB = sA + A_STAGE;
     const int k0 = kb * kBK;
-    if (a_vec) {
-      constexpr int CH = BM * kBK / 4;
-#pragma unroll
-      for (int c0 = 0; c0 < CH; c0 += kThreads) {
-        const int c = c0 + tid;
-        if (CH % kThreads == 0 || c < CH) {
-          const int mm = (c % (BM / 4)) * 4, kk = c / (BM / 4);
-          const int gm = m0 + mm, gk = k0 + kk;
-          int valid = (gk < K) ? min(max(M - gm, 0), 4) : 0;
-          const float* src = valid ? A + gk * lda + gm : A;
-          cp_async16(smem_u32(sA + kk * BM + mm), src, valid * 4);
-        }
-      }
-    } else {
-      constexpr int EL = BM * kBK;
-#pragma unroll
-      for (int e0 = 0; e0 < EL; e0 += kThreads) {
-        const int e = e0 + tid;
-        if (EL % kThreads == 0 || e < EL) {
-          const int mm = e % BM, kk = e / BM;
-          const int gm = m0 + mm, gk = k0 + kk;
-          const bool v = (gk < K) && (gm < M);
-          cp_async4(smem_u32(sA + kk * BM + mm), v ? A + gk * lda + gm : A, v ? 4 : 0);
-        }
-      }
-    }
-    constexpr int EB = BN * kBK;
-#pragma unroll
-    for (int e0 = 0; e0 < EB; e0 += kThreads) {
-      const int e = e0 + tid;
-      if (EB % kThreads == 0 || e < EB) {
-        const int kk = e % kBK, nn = e / kBK;
-        const int gk = k0 + kk, gn = n0 + nn;
-        const bool v = (gk < K) && (gn < N);
-        cp_async4(smem_u32(sB + kk * LDBS + nn), v ? B + gn * ldb + gk : B, v ? 4 : 0);
-      }
-    }
+    if (!ta)
+      load_rows_contig<BM, LDAS>(A, lda, M, m0, k0, K, sA, a_vec, tid);
+    else
+      load_k_contig<BM, LDAS>(A, lda, M, m0, k0, K, sA, tid);
+    if (tb)
+      load_rows_contig<BN, LDBS>(B, ldb, N, n0, k0, K, sB, b_vec, tid);
+    else
+      load_k_contig<BN, LDBS>(B, ldb, N, n0, k0, K, sB, tid);
   };
 
 #pragma unroll
@@ -184,7 +212,7 @@ __device__ __forceinline__ void simt_tile(const MatDesc& d, int tm, int tn,
     for (int k = 0; k < kBK; ++k) {
       float a[TM], b[TN];
 #pragma unroll
-      for (int h = 0; h < HM; ++h) VecLd<TMH>::ld(sA + k * BM + h * (BM / HM) + tx * TMH, a + h * TMH);
+      for (int h = 0; h < HM; ++h) VecLd<TMH>::ld(sA + k * LDAS + h * (BM / HM) + tx * TMH, a + h * TMH);
 #pragma unroll
       for (int h = 0; h < HN; ++h) VecLd<TNH>::ld(sB + k * LDBS + h * (BN / HN) + ty * TNH, b + h * TNH);
 #pragma unroll

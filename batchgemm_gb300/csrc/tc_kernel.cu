@@ -138,12 +138,18 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
     const PackDesc pd = p.pdescs[job.mat];
     const int K = d.K;
     const long long kpad = pd.kpad;
-    if (job.op == 0) {
-      // A (column-major M x K) -> rows m of K: transpose through shared memory
-      const float* A = p.A[job.mat];
-      const long long lda = d.lda;
-      char* hi = p.ws + pd.a_hi;
-      char* lo = p.ws + pd.a_lo;
+    // the strip's source: op(A) rows m or op(B)^T rows n, element (r, k) at
+    // X[r + k*ldx] ("rows contiguous": A, or B stored transposed) or at
+    // X[k + r*ldx] ("k contiguous": B, or A stored transposed)
+    const bool is_a = job.op == 0;
+    const float* X = is_a ? p.A[job.mat] : p.B[job.mat];
+    const long long ldx = is_a ? d.lda : d.ldb;
+    const int rows = is_a ? d.M : d.N;
+    const bool rows_contig = is_a ? !(d.aux & kTransAFlag) : (d.aux & kTransBFlag) != 0;
+    char* hi = p.ws + (is_a ? pd.a_hi : pd.b_hi);
+    char* lo = p.ws + (is_a ? pd.a_lo : pd.b_lo);
+    if (rows_contig) {
+      // transpose through shared memory: loads walk 32 consecutive rows
       const int mm = tid & 31;
       const int m = job.r0 + mm;
       for (int k0 = 0; k0 < K; k0 += 64) {
@@ -151,7 +157,7 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
           const int k = k0 + (tid >> 5) + 8 * i;
-          v[i] = (m < d.M && k < K) ? A[m + k * lda] : 0.0f;
+          v[i] = (m < rows && k < K) ? X[m + k * ldx] : 0.0f;
         }
 #pragma unroll
         for (int i = 0; i < 8; ++i) t[(tid >> 5) + 8 * i][mm] = v[i];
@@ -163,7 +169,7 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
           const int kk = wk + 32 * h2;
           const int k = k0 + kk;
           const int mr = job.r0 + wm;
-          if (mr < d.M && k < K) {
+          if (mr < rows && k < K) {
             float x[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) x[i] = t[kk + i][wm];
@@ -178,16 +184,12 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
         __syncthreads();
       }
     } else {
-      // B (column-major K x N) is already rows n of K
-      const float* B = p.B[job.mat];
-      const long long ldb = d.ldb;
-      char* hi = p.ws + pd.b_hi;
-      char* lo = p.ws + pd.b_lo;
+      // already rows of K: 8 threads per row, four consecutive k each
       const int nn = tid >> 3;
       const int n = job.r0 + nn;
       const int wk = (tid & 7) * 4;
-      if (n >= d.N) continue;
-      const float* col = B + n * ldb;
+      if (n >= rows) continue;
+      const float* col = X + n * ldx;
       const bool vec = ((reinterpret_cast<uintptr_t>(col) & 15u) == 0);
       for (int k0 = 0; k0 < K; k0 += 64) {
         float x[2][4];

@@ -149,7 +149,7 @@ void tc_tile_dims(bgemm_plan_s* p, int, int, int, int cfg, int* bm, int* bn, Mat
   const bool pair = p->tc->pair;
   *bm = pair ? 256 : kTcBM;
   *bn = pair ? tc2_cfg_bn(cfg) : tc_cfg_bn(cfg);
-  d->aux = tc_cfg_swap(cfg) ? kTcSwapFlag : 0;
+  d->aux = (d->aux & ~kTcSwapFlag) | (tc_cfg_swap(cfg) ? kTcSwapFlag : 0);
 }
 
 // Workspace: per matrix [A hi][A lo][B hi][B lo], rows of kpad elements;

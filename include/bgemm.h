@@ -68,6 +68,16 @@ typedef enum bgemm_mode {
   BGEMM_MODE_BF16X3 = 3     /* tcgen05 kind::f16 (bf16), 3-product split    */
 } bgemm_mode_t;
 
+/* Storage order of every matrix of a call and per-operand transposition
+ * (BLAS / magma vbatched convention: C = alpha * op(A) * op(B) + beta * C,
+ * op(A) is M x K, op(B) is K x N).  Column-major: A (N) is M x K with
+ * lda >= M, A (T) is stored K x M with lda >= K; B (N) is K x N with
+ * ldb >= K, B (T) is stored N x K with ldb >= N; ldc >= M.  Row-major: the
+ * same matrices stored by rows, so lda >= K (A N) or M (A T), ldb >= N (B N)
+ * or K (B T), ldc >= N. */
+typedef enum bgemm_layout { BGEMM_COL_MAJOR = 0, BGEMM_ROW_MAJOR = 1 } bgemm_layout_t;
+typedef enum bgemm_op { BGEMM_OP_N = 0, BGEMM_OP_T = 1 } bgemm_op_t;
+
 typedef struct bgemm_plan_s* bgemm_plan_t;
 
 /* Per-plan facts (for benchmarks and tests). */
@@ -112,7 +122,10 @@ typedef struct bgemm_plan_options {
                                it is off by default (kept for comparison). */
   int kernel_family;        /* split tensor-core modes: 0 chosen by the cost
                                model, 1 one-SM tiles, 2 CTA-pair tiles        */
-  int reserved[5];
+  int layout;               /* bgemm_layout_t of every matrix (0: column-major) */
+  int trans_a;              /* bgemm_op_t applied to every A (0: N)          */
+  int trans_b;              /* bgemm_op_t applied to every B (0: N)          */
+  int reserved[2];
   /* Capacity for bgemm_plan_update: each field is raised to the creating
    * batch's own requirement, so all-zero means "this batch only".
    * kernel_family is ignored here (see the field above). */
@@ -132,6 +145,22 @@ bgemm_status_t bgemm_sgemm_vbatched(const int* M, const int* N, const int* K,
                                     float* const* dC, const int* ldc,
                                     int batch, bgemm_mode_t mode,
                                     bgemm_stream_t stream);
+
+/* Same as bgemm_sgemm_vbatched with a storage order and op(A), op(B) (see
+ * bgemm_layout_t).  The FP32 SIMT mode stays one fma chain per element over
+ * k in order, so the result is bit-identical to the column-major NN call on
+ * the materialised op(A), op(B).  Row-major calls run as the column-major
+ * product C^T = op(B)^T op(A)^T on the same memory (no copies).  Argument
+ * numbers: layout 1, transA 2, transB 3, M 4, N 5, K 6, alpha 7, dA 8,
+ * lda 9, dB 10, ldb 11, beta 12, dC 13, ldc 14, batch 15, mode 16. */
+bgemm_status_t bgemm_sgemm_vbatched_ex(bgemm_layout_t layout, bgemm_op_t transA,
+                                       bgemm_op_t transB, const int* M,
+                                       const int* N, const int* K, float alpha,
+                                       const float* const* dA, const int* lda,
+                                       const float* const* dB, const int* ldb,
+                                       float beta, float* const* dC,
+                                       const int* ldc, int batch,
+                                       bgemm_mode_t mode, bgemm_stream_t stream);
 
 /* --- plan / execute split (execute allocates nothing: capturable) --------- */
 bgemm_status_t bgemm_plan_create(bgemm_plan_t* plan, const int* M,

@@ -202,3 +202,37 @@ def test_option_structs_match_the_header(tmp_path):
         assert got[(cname, "sizeof")] == ctypes.sizeof(py), cname
         for f in py._fields_:
             assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])
+
+
+@pytest.mark.parametrize("layout,ta,tb,bad,argpos", [
+    ("col", "T", "N", "lda", 9),   # A stored K x M: lda >= K
+    ("col", "N", "T", "ldb", 11),  # B stored N x K: ldb >= N
+    ("row", "N", "N", "lda", 9),   # row-major A (M x K): lda >= K
+    ("row", "N", "N", "ldc", 14),  # row-major C (M x N): ldc >= N
+    ("row", "T", "T", "ldb", 11),  # row-major B^T stored N x K: ldb >= K
+])
+def test_layout_trans_leading_dimension_rules(built_lib, layout, ta, tb, bad, argpos):
+    """bgemm_sgemm_vbatched_ex checks each leading dimension against the extent
+    it spans for the given storage order and op, before any device work."""
+    M, N, K = [7, 9], [5, 30], [11, 20]
+    ext = {"col": {"lda": lambda i: K[i] if ta == "T" else M[i],
+                   "ldb": lambda i: N[i] if tb == "T" else K[i], "ldc": lambda i: M[i]},
+           "row": {"lda": lambda i: M[i] if ta == "T" else K[i],
+                   "ldb": lambda i: K[i] if tb == "T" else N[i], "ldc": lambda i: N[i]}}[layout]
+    ld = {k: [ext[k](i) for i in range(2)] for k in ("lda", "ldb", "ldc")}
+    ld[bad][1] -= 1
+    with pytest.raises(bg.BgemmError) as ei:
+        bg.sgemm_vbatched_ex(layout, ta, tb, M, N, K, 1.0, 1, ld["lda"], 1, ld["ldb"], 0.0, 1,
+                             ld["ldc"])
+    assert ei.value.status == 1 and ei.value.arg == argpos and ei.value.matrix == 1
+
+
+def test_layout_trans_enum_values_rejected(built_lib):
+    L = bg.lib()
+    one = bg.int_array([1])
+    assert L.bgemm_sgemm_vbatched_ex(2, 0, 0, one, one, one, 1.0, None, one, None, one, 0.0,
+                                     None, one, 1, 0, None) == 1
+    assert L.bgemm_last_error_arg(None) == 1
+    assert L.bgemm_sgemm_vbatched_ex(0, 0, 5, one, one, one, 1.0, None, one, None, one, 0.0,
+                                     None, one, 1, 0, None) == 1
+    assert L.bgemm_last_error_arg(None) == 3
