@@ -22,6 +22,8 @@ INC = os.path.join(ROOT, "include")
 # machine never links the other machine's objects
 BUILD = os.path.join(PKG, "_build", platform.machine())
 LIB = os.path.join(PKG, "libbgemm_gb300.so")
+CLI_SRC = os.path.join(PKG, "cli", "bgemm_gemm.cpp")
+CLI = os.path.join(PKG, "bgemm_gemm")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -106,7 +108,30 @@ def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = Fals
         os.replace(tmp, LIB)
         with open(stamp, "w") as f:
             f.write(platform.machine() + "\n")
+    build_cli(cuda, verbose, force)
     return LIB
+
+
+def build_cli(cuda: str, verbose: bool = False, force: bool = False) -> str:
+    """The reference-compatible command-line benchmark (cli/bgemm_gemm.cpp),
+    linked against the library next to it."""
+    stamp = os.path.join(BUILD, "cli.stamp")
+    deps = [CLI_SRC, LIB, os.path.join(INC, "bgemm.h")]
+    if not force and os.path.exists(CLI) and not _stale(stamp, deps):
+        return CLI
+    tmp = CLI + ".tmp%d" % os.getpid()
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", INC, "-I", os.path.join(cuda, "include"),
+           CLI_SRC, "-o", tmp, "-L", PKG, "-lbgemm_gb300", "-L", os.path.join(cuda, "lib64"),
+           "-lcudart", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("CLI build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, CLI)
+    with open(stamp, "w") as f:
+        f.write(platform.machine() + "\n")
+    return CLI
 
 
 if __name__ == "__main__":

@@ -49,7 +49,9 @@ struct SimtParams {
   float* const* C;
 };
 
-cudaError_t simt_launch(const SimtParams& p, int grid, cudaStream_t stream);
+// transposed: the plan's matrices carry kTransAFlag / kTransBFlag
+cudaError_t simt_launch(const SimtParams& p, int grid, cudaStream_t stream,
+                        bool transposed = false);
 int simt_ctas_per_sm();
 
 }  // namespace bgemm

@@ -579,7 +579,7 @@ bgemm_status_t plan_execute(bgemm_plan_t p, float alpha, const float* const* dA,
     SimtParams sp{p->d_descs, p->d_items,  p->n_items, p->d_counters + kHdrItems,
                   p->d_counters, alpha,    beta,       dA, dB, dC};
     if (p->ev_start) cudaEventRecord(p->ev_start, stream);
-    cudaError_t e = simt_launch(sp, p->grid, stream);
+    cudaError_t e = simt_launch(sp, p->grid, stream, p->aux_trans != 0);
     if (p->ev_stop) cudaEventRecord(p->ev_stop, stream);
     if (e != cudaSuccess) return cuda_error(e, "SIMT launch");
     return BGEMM_SUCCESS;

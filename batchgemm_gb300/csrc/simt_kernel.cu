@@ -9,13 +9,15 @@
 //
 // Each item is one BM x BN output tile of one matrix.  256 threads form a
 // 16 x 16 grid; each owns a TM x TN register tile.  Operands stream through a
-// 4-stage cp.async ring of BK = 8 k-slices, [k][BM + 4] for op(A) and
-// [k][BN + 4] for op(B).  An operand whose rows of the slice are contiguous
-// in memory (A column-major, or B stored transposed) is copied with 16-byte
-// cp.async when its leading dimension and base allow it, else 4-byte; an
-// operand contiguous along k (B column-major, or A stored transposed) is
-// transposed on the way in by 4-byte cp.async (the +4 pad keeps the
-// scattered shared-memory writes conflict-free).
+// 4-stage cp.async ring of BK = 8 k-slices:
+//   A slice: [k][BM]     (column of A, 16-byte cp.async when lda % 4 == 0 and
+//                         A is 16-byte aligned, 4-byte otherwise)
+//   B slice: [k][BN + 4] (transposed on the way in by 4-byte cp.async; the
+//                         +4 pad keeps the scattered writes conflict-free)
+// Plans with transposed operands run simt_persistent_kernel_t: an operand
+// whose slice rows are contiguous in memory (A, or B stored N x K) takes the
+// A path above, one contiguous along k (B, or A stored K x M) the B path, and
+// the A slice is padded to [k][BM + 4] as well.
 // Edges are zero-filled by the cp.async source size, so any M, N, K >= 0 and
 // any leading dimension work.  Every output element is a single fma chain
 // over k in order (bit-exact with the reference's tile bodies and with the
@@ -33,8 +35,9 @@ constexpr int kThreads = 256;
 constexpr int kBK = 8;
 constexpr int kStages = 4;
 constexpr int kPadB = 4;
-constexpr int kMaxStageFloats = kBK * (128 + kPadB + 128 + kPadB);
+constexpr int kMaxStageFloats = kBK * (128 + 128 + kPadB);
 constexpr int kSmemBytes = kStages * kMaxStageFloats * 4;
+constexpr int kSmemBytesT = kStages * kBK * (128 + kPadB + 128 + kPadB) * 4;  // transposed kernel
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -130,7 +133,9 @@ __device__ __forceinline__ void load_k_contig(const float* X, long long ldx, int
   }
 }
 
-template <int BM, int BN, int TM, int TN>
+// GEN = false: the reference's layout (A and B untransposed), fixed at
+// compile time; GEN = true: per-matrix transposition flags.
+template <int BM, int BN, int TM, int TN, bool GEN = false>
 __device__ __forceinline__ void simt_tile(const MatDesc& d, int tm, int tn,
                                           const float* __restrict__ A,
                                           const float* __restrict__ B, float* __restrict__ C,
@@ -142,8 +147,8 @@ __device__ __forceinline__ void simt_tile(const MatDesc& d, int tm, int tn,
   constexpr int TNH = TN > 4 ? 4 : TN;
   constexpr int HM = TM / TMH;          // halves along m (2 for TM = 8)
   constexpr int HN = TN / TNH;
-  constexpr int LDAS = BM + kPadB;
   constexpr int LDBS = BN + kPadB;
+  constexpr int LDAS = GEN ? BM + kPadB : BM;
   constexpr int A_STAGE = kBK * LDAS;
   constexpr int STAGE = A_STAGE + kBK * LDBS;
 
@@ -174,22 +179,65 @@ __device__ __forceinline__ void simt_tile(const MatDesc& d, int tm, int tn,
     }
 
   const int nkb = (K + kBK - 1) / kBK;
-  const bool ta = (d.aux & kTransAFlag) != 0, tb = (d.aux & kTransBFlag) != 0;
-  const bool a_vec = !ta && ((reinterpret_cast<uintptr_t>(A) & 15u) == 0) && ((d.lda & 3) == 0);
-  const bool b_vec = tb && ((reinterpret_cast<uintptr_t>(B) & 15u) == 0) && ((d.ldb & 3) == 0);
+  const bool a_vec = ((reinterpret_cast<uintptr_t>(A) & 15u) == 0) && ((d.lda & 3) == 0) &&
+                     !(GEN && (d.aux & kTransAFlag));
 
   auto load_stage = [&](int kb, int slot) {
     float* sA = smem + slot * STAGE;
     float* sB = sA + A_STAGE;
     const int k0 = kb * kBK;
-    if (!ta)
-      load_rows_contig<BM, LDAS>(A, lda, M, m0, k0, K, sA, a_vec, tid);
-    else
-      load_k_contig<BM, LDAS>(A, lda, M, m0, k0, K, sA, tid);
-    if (tb)
-      load_rows_contig<BN, LDBS>(B, ldb, N, n0, k0, K, sB, b_vec, tid);
-    else
-      load_k_contig<BN, LDBS>(B, ldb, N, n0, k0, K, sB, tid);
+    if constexpr (GEN) {
+      const bool ta = (d.aux & kTransAFlag) != 0, tb = (d.aux & kTransBFlag) != 0;
+      if (!ta)
+        load_rows_contig<BM, LDAS>(A, lda, M, m0, k0, K, sA, a_vec, tid);
+      else
+        load_k_contig<BM, LDAS>(A, lda, M, m0, k0, K, sA, tid);
+      if (tb)
+        load_rows_contig<BN, LDBS>(B, ldb, N, n0, k0, K, sB,
+                                   ((reinterpret_cast<uintptr_t>(B) & 15u) == 0) &&
+                                       ((d.ldb & 3) == 0),
+                                   tid);
+      else
+        load_k_contig<BN, LDBS>(B, ldb, N, n0, k0, K, sB, tid);
+      return;
+    }
+    if (a_vec) {
+      constexpr int CH = BM * kBK / 4;
+#pragma unroll
+      for (int c0 = 0; c0 < CH; c0 += kThreads) {
+        const int c = c0 + tid;
+        if (CH % kThreads == 0 || c < CH) {
+          const int mm = (c % (BM / 4)) * 4, kk = c / (BM / 4);
+          const int gm = m0 + mm, gk = k0 + kk;
+          int valid = (gk < K) ? min(max(M - gm, 0), 4) : 0;
+          const float* src = valid ? A + gk * lda + gm : A;
+          cp_async16(smem_u32(sA + kk * BM + mm), src, valid * 4);
+        }
+      }
+    } else {
+      constexpr int EL = BM * kBK;
+#pragma unroll
+      for (int e0 = 0; e0 < EL; e0 += kThreads) {
+        const int e = e0 + tid;
+        if (EL % kThreads == 0 || e < EL) {
+          const int mm = e % BM, kk = e / BM;
+          const int gm = m0 + mm, gk = k0 + kk;
+          const bool v = (gk < K) && (gm < M);
+          cp_async4(smem_u32(sA + kk * BM + mm), v ? A + gk * lda + gm : A, v ? 4 : 0);
+        }
+      }
+    }
+    constexpr int EB = BN * kBK;
+#pragma unroll
+    for (int e0 = 0; e0 < EB; e0 += kThreads) {
+      const int e = e0 + tid;
+      if (EB % kThreads == 0 || e < EB) {
+        const int kk = e % kBK, nn = e / kBK;
+        const int gk = k0 + kk, gn = n0 + nn;
+        const bool v = (gk < K) && (gn < N);
+        cp_async4(smem_u32(sB + kk * LDBS + nn), v ? B + gn * ldb + gk : B, v ? 4 : 0);
+      }
+    }
   };
 
 #pragma unroll
@@ -328,17 +376,62 @@ __global__ void __launch_bounds__(kThreads, 2) simt_persistent_kernel(const Simt
   }
 }
 
+// The same persistent loop for plans whose matrices carry kTransAFlag /
+// kTransBFlag (kept apart so the untransposed kernel above stays as it is).
+__global__ void __launch_bounds__(kThreads, 2) simt_persistent_kernel_t(const SimtParams p) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ int s_item;
+  const int n_items = p.n_items_dev ? *p.n_items_dev : p.n_items;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(p.counters, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= n_items) break;
+    const TileItem ti = p.items[it];
+    const MatDesc d = p.descs[ti.mat];
+    const float* A = p.A[ti.mat];
+    const float* B = p.B[ti.mat];
+    float* C = p.C[ti.mat];
+    switch (d.cfg) {
+      case 0: simt_tile<16, 16, 1, 1, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 1: simt_tile<32, 32, 2, 2, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 2: simt_tile<64, 32, 4, 2, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 3: simt_tile<32, 64, 2, 4, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 4: simt_tile<64, 64, 4, 4, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 5: simt_tile<128, 64, 8, 4, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 6: simt_tile<64, 128, 4, 8, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      default: simt_tile<128, 128, 8, 8, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(reinterpret_cast<unsigned*>(p.counters) + 1, 1u);
+    if (prev == gridDim.x - 1) {
+      atomicExch(p.counters, 0);
+      atomicExch(p.counters + 1, 0);
+      __threadfence();
+    }
+  }
+}
+
 }  // namespace
 
-cudaError_t simt_launch(const SimtParams& p, int grid, cudaStream_t stream) {
+cudaError_t simt_launch(const SimtParams& p, int grid, cudaStream_t stream, bool transposed) {
   static bool attr_done = false;
   if (!attr_done) {
     cudaError_t e = cudaFuncSetAttribute(simt_persistent_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(simt_persistent_kernel_t,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytesT);
     if (e != cudaSuccess) return e;
     attr_done = true;
   }
-  simt_persistent_kernel<<<grid, kThreads, kSmemBytes, stream>>>(p);
+  if (transposed)
+    simt_persistent_kernel_t<<<grid, kThreads, kSmemBytesT, stream>>>(p);
+  else
+    simt_persistent_kernel<<<grid, kThreads, kSmemBytes, stream>>>(p);
   return cudaGetLastError();
 }
 
@@ -349,6 +442,12 @@ int simt_ctas_per_sm() {
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, simt_persistent_kernel, kThreads,
                                                     kSmemBytes) != cudaSuccess)
     return 1;
+  int nt = 0;
+  cudaFuncSetAttribute(simt_persistent_kernel_t, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       kSmemBytesT);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nt, simt_persistent_kernel_t, kThreads,
+                                                    kSmemBytesT) == cudaSuccess && nt < n)
+    n = nt;  // plans size their grid before they know which kernel runs
   return n > 0 ? n : 1;
 }
 
