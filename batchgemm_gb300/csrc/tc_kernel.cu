@@ -124,12 +124,15 @@ __device__ __forceinline__ void put4(char* hi, char* lo, long long idx, const fl
   }
 }
 
-// One job = 32 packed rows of one operand, walked in chunks of 64 k.  Each
-// thread issues all eight of its loads for a chunk before it stores, and
+// k per chunk of the pre-pass: each thread keeps kPackK / 8 loads in flight.
+constexpr int kPackK = 128;
+
+// One job = 32 packed rows of one operand, walked in chunks of kPackK k.  Each
+// thread issues all kPackK / 8 of its loads for a chunk before it stores, and
 // writes four consecutive k per store (rows are 16-byte aligned, so packed
 // writes are full vectors; the K tail and rows past M/N are masked).
 __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
-  __shared__ float t[64][33];
+  __shared__ float t[kPackK][33];
   const int tid = threadIdx.x;
   const int n_jobs = p.n_jobs_dev ? *p.n_jobs_dev : p.n_jobs;
   for (int j = blockIdx.x; j < n_jobs; j += gridDim.x) {
@@ -152,20 +155,20 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
       // transpose through shared memory: loads walk 32 consecutive rows
       const int mm = tid & 31;
       const int m = job.r0 + mm;
-      for (int k0 = 0; k0 < K; k0 += 64) {
-        float v[8];
+      for (int k0 = 0; k0 < K; k0 += kPackK) {
+        float v[kPackK / 8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < kPackK / 8; ++i) {
           const int k = k0 + (tid >> 5) + 8 * i;
           v[i] = (m < rows && k < K) ? X[m + k * ldx] : 0.0f;
         }
 #pragma unroll
-        for (int i = 0; i < 8; ++i) t[(tid >> 5) + 8 * i][mm] = v[i];
+        for (int i = 0; i < kPackK / 8; ++i) t[(tid >> 5) + 8 * i][mm] = v[i];
         __syncthreads();
         const int wm = tid >> 3;           // packed row within the strip
         const int wk = (tid & 7) * 4;      // first of four k
 #pragma unroll
-        for (int h2 = 0; h2 < 2; ++h2) {
+        for (int h2 = 0; h2 < kPackK / 32; ++h2) {
           const int kk = wk + 32 * h2;
           const int k = k0 + kk;
           const int mr = job.r0 + wm;
@@ -191,10 +194,10 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
       if (n >= rows) continue;
       const float* col = X + n * ldx;
       const bool vec = ((reinterpret_cast<uintptr_t>(col) & 15u) == 0);
-      for (int k0 = 0; k0 < K; k0 += 64) {
-        float x[2][4];
+      for (int k0 = 0; k0 < K; k0 += kPackK) {
+        float x[kPackK / 32][4];
 #pragma unroll
-        for (int h2 = 0; h2 < 2; ++h2) {
+        for (int h2 = 0; h2 < kPackK / 32; ++h2) {
           const int k = k0 + wk + 32 * h2;
           if (vec && k + 4 <= K) {
             const float4 f = *reinterpret_cast<const float4*>(col + k);
@@ -205,7 +208,7 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
           }
         }
 #pragma unroll
-        for (int h2 = 0; h2 < 2; ++h2) {
+        for (int h2 = 0; h2 < kPackK / 32; ++h2) {
           const int k = k0 + wk + 32 * h2;
           if (k + 4 <= K) {
             put4(hi, lo, n * kpad + k, x[h2], p.kind, p.split);
