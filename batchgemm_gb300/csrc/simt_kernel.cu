@@ -178,6 +178,17 @@ __device__ __forceinline__ void simt_tile(const MatDesc& d, int tm, int tn,
       acc[i][j] = v;
     }
 
+  if (!inplace && beta != 0.0f) {
+#pragma unroll
+    for (int j = 0; j < TN; ++j)
+#pragma unroll
+      for (int h = 0; h < HM; ++h) {
+        const int n = col_of(j), mb = m0 + h * (BM / HM) + tx * TMH;
+        if (n < N && mb < M)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(C + n * ldc + mb));
+      }
+  }
+
   const int nkb = (K + kBK - 1) / kBK;
   const bool a_vec = ((reinterpret_cast<uintptr_t>(A) & 15u) == 0) && ((d.lda & 3) == 0) &&
                      !(GEN && (d.aux & kTransAFlag));
@@ -272,9 +283,57 @@ __device__ __forceinline__ void simt_tile(const MatDesc& d, int tm, int tn,
   cp_async_wait<0>();
 
   // ---- epilogue ----
+  const int lane = tid & 31;
+  if (!inplace && beta != 0.0f) {
+    // C is read: the lines were prefetched into L2 when the tile started.
+    // Columns go two at a time, all reads of a pair before its writes (a
+    // write may alias a later read as far as the compiler knows, so
+    // interleaving them would serialise one memory round trip per element);
+    // rows use the half-warp transpose below so accesses are 64-byte runs.
+    constexpr int CJ = TN < 2 ? TN : 2;
+#pragma unroll
+    for (int jc = 0; jc < TN; jc += CJ) {
+      float x[CJ][HM][TMH], cv[CJ][HM][TMH];
+#pragma unroll
+      for (int jj = 0; jj < CJ; ++jj)
+#pragma unroll
+        for (int h = 0; h < HM; ++h)
+#pragma unroll
+          for (int q = 0; q < TMH; ++q) {
+            const int ml = q * 16 + tx;
+            const int src = (lane & 16) | (ml / TMH);
+            const int rsel = ml % TMH;
+            float t = 0.0f;
+#pragma unroll
+            for (int r = 0; r < TMH; ++r) {
+              const float u = __shfl_sync(0xffffffffu, acc[h * TMH + r][jc + jj], src);
+              if (r == rsel) t = u;
+            }
+            x[jj][h][q] = t;
+          }
+#pragma unroll
+      for (int jj = 0; jj < CJ; ++jj)
+#pragma unroll
+        for (int h = 0; h < HM; ++h)
+#pragma unroll
+          for (int q = 0; q < TMH; ++q) {
+            const int n = col_of(jc + jj), m = m0 + h * (BM / HM) + q * 16 + tx;
+            cv[jj][h][q] = (n < N && m < M) ? C[n * ldc + m] : 0.0f;
+          }
+#pragma unroll
+      for (int jj = 0; jj < CJ; ++jj)
+#pragma unroll
+        for (int h = 0; h < HM; ++h)
+#pragma unroll
+          for (int q = 0; q < TMH; ++q) {
+            const int n = col_of(jc + jj), m = m0 + h * (BM / HM) + q * 16 + tx;
+            if (n < N && m < M) C[n * ldc + m] = fmaf(alpha, x[jj][h][q], beta * cv[jj][h][q]);
+          }
+    }
+    return;
+  }
   const bool c_vec = (TMH == 4) && ((reinterpret_cast<uintptr_t>(C) & 15u) == 0) &&
                      ((d.ldc & 3) == 0);
-  const int lane = tid & 31;
 #pragma unroll
   for (int j = 0; j < TN; ++j) {
     const int n = col_of(j);

@@ -197,9 +197,9 @@ def cpu_sample(w, budget_s=15.0, threads=None):
 
 
 # ---------------------------------------------------------------- GPU leg --
-def fp64_sampled_error(db, per_matrix=4, seed=0, C0=None, beta=0.0):
-    """Normalised error |c - c64| / (sum|a b| + |beta c0|) on sampled entries,
-    FP64 on the GPU (C0: the C buffer before the step, when beta != 0)."""
+def fp64_sampled_error(db, per_matrix=4, seed=0, C0=None, beta=0.0, alpha=1.0):
+    """Normalised error |c - c64| / (|alpha| sum|a b| + |beta c0|) on sampled
+    entries, FP64 on the GPU (C0: the C buffer before the step, when beta != 0)."""
     import torch
     rng = np.random.default_rng(seed)
     idx_m, idx_n, mats = [], [], []
@@ -229,8 +229,8 @@ def fp64_sampled_error(db, per_matrix=4, seed=0, C0=None, beta=0.0):
         a = db.A[offA[:, None] + ka * lda[:, None]].double()
         b = db.B[offB[:, None] + ka].double()
         prod = torch.where(mask, a * b, torch.zeros_like(a))
-        exact = prod.sum(1)
-        absb = prod.abs().sum(1)
+        exact = alpha * prod.sum(1)
+        absb = abs(alpha) * prod.abs().sum(1)
         offC = torch.tensor([db.offC[mats[s]] + idx_m[s] + idx_n[s] * db.ldc[mats[s]]
                              for s in ss], device=dev)
         c = db.C[offC].double()
@@ -261,6 +261,14 @@ def gpu_leg(args, rank, world, local):
     if os.path.exists(pk_path):
         peaks = json.load(open(pk_path))
     num_sms = bg.device_info()["num_sms"]
+
+    def one_step_error(plan):
+        """Error of one execute from a snapshot of C (the timed steps have
+        accumulated beta * C into it)."""
+        C0 = db.C.clone() if w.beta != 0 else None
+        db.execute(plan, w.alpha, w.beta, stream=s)
+        s.synchronize()
+        return fp64_sampled_error(db, C0=C0, beta=w.beta, alpha=w.alpha)
 
     def time_mode(mode, steps, warmup, sample_clocks=False):
         with torch.cuda.stream(s):
@@ -303,7 +311,7 @@ def gpu_leg(args, rank, world, local):
     out = {}
     plan, info, ms, clocks = time_mode(args.mode, args.steps, args.warmup, sample_clocks=True)
     value, ms_max = whole_job_tflops(flops, ms, world, dev)
-    err_max, err_mean, nsamp = fp64_sampled_error(db)
+    err_max, err_mean, nsamp = one_step_error(plan)
     out.update(value=value, ms=ms_max, info=info, clocks=clocks, err=(err_max, err_mean, nsamp),
                launches=info["kernels_per_execute"] * args.steps)
     # the dominant (GEMM) kernel alone: events recorded by the library around
@@ -333,7 +341,7 @@ def gpu_leg(args, rank, world, local):
                 continue
             try:
                 p2, inf2, ms2, _ = time_mode(mode, max(3, args.steps // 4), 3)
-                e2 = fp64_sampled_error(db)
+                e2 = one_step_error(p2)
                 extra[mode] = {"tflops": round(flops / (ms2 * 1e-3) / 1e12, 3),
                                "ms_per_step": round(ms2, 4),
                                "err_vs_fp64_max": e2[0], "err_vs_fp64_mean": e2[1]}
