@@ -32,7 +32,7 @@ namespace bgemm {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kBK = 8;
+constexpr int kBK = 16;
 constexpr int kStages = 4;
 constexpr int kPadB = 4;
 constexpr int kMaxStageFloats = kBK * (128 + 128 + kPadB);
