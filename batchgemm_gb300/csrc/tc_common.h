@@ -97,6 +97,9 @@ struct TcTmapParams {
 };
 
 cudaError_t tc_pack_launch(const TcPackParams& p, int grid, cudaStream_t s);
+// one CTA waiting on a barrier that never completes (bounded-wait self-test)
+cudaError_t tc_wait_selftest_launch(int* err, int* out, unsigned long long limit_ns,
+                                    cudaStream_t s);
 cudaError_t tc_tmap_launch(const TcTmapParams& p, cudaStream_t s);
 cudaError_t tc_gemm_launch(int kind, int split, const TcGemmParams& p, int grid, cudaStream_t s);
 int tc_smem_bytes(int kind, int split);

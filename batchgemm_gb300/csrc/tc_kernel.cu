@@ -589,7 +589,34 @@ cudaError_t launch_gemm(const TcGemmParams& p, int grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Self-test of the bounded mbarrier wait every tensor-core kernel uses: one
+// CTA waits on a barrier that nothing will ever arrive on.  The wait must
+// give up after limit_ns, set bit 0 of *err, and let the kernel return;
+// out[0] = 1 records that the thread got past the wait, out[1] the wait's
+// result (0 = gave up).
+__global__ void bounded_wait_selftest_kernel(int* err, int* out, unsigned long long limit_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(&bar), 1);
+    abort_flag = 0;
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const bool ok = wait_bounded(smem_u32(&bar), 0, err, &abort_flag, limit_ns);
+    out[1] = ok ? 1 : 0;
+    out[0] = 1;
+  }
+}
+
 }  // namespace
+
+cudaError_t tc_wait_selftest_launch(int* err, int* out, unsigned long long limit_ns,
+                                    cudaStream_t s) {
+  bounded_wait_selftest_kernel<<<1, 32, 0, s>>>(err, out, limit_ns);
+  return cudaGetLastError();
+}
 
 cudaError_t tc_tmap_launch(const TcTmapParams& p, cudaStream_t s) {
   if (p.batch == 0) return cudaSuccess;

@@ -8,6 +8,7 @@
 
 #include <cudaTypedefs.h>
 
+#include "bgemm_debug.h"
 #include "plan_internal.h"
 #include "tc_common.h"
 #include "tile_table.h"
@@ -420,3 +421,21 @@ void tc_plan_release(bgemm_plan_s* p) {
 }
 
 }  // namespace bgemm
+
+extern "C" int bgemm_debug_bounded_wait_selftest(unsigned long long limit_ns, int* error,
+                                                 int* returned, int* wait_ok) {
+  using namespace bgemm;
+  int* d = nullptr;
+  if (cudaMalloc(&d, 4 * sizeof(int)) != cudaSuccess) return -1;
+  int h[4] = {0, 0, 0, 0};
+  cudaError_t e = cudaMemset(d, 0, 4 * sizeof(int));
+  if (e == cudaSuccess) e = tc_wait_selftest_launch(d, d + 1, limit_ns, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return -1;
+  if (error) *error = h[0];
+  if (returned) *returned = h[1];
+  if (wait_ok) *wait_ok = h[2];
+  return 0;
+}

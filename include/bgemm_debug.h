@@ -33,6 +33,17 @@ int bgemm_debug_simt_queue(const int* M, const int* N, const int* K, int batch, 
 int bgemm_debug_compare_tensor_maps(void* plan, void* stream, int* n_maps, int* n_diff,
                                     int* first_byte);
 
+/* Self-test of the bounded device-side wait used by every tensor-core
+ * kernel (no counterpart in the reference, whose kernels have no device
+ * waits): one CTA waits on an mbarrier that nothing arrives on.  The wait
+ * must expire after limit_ns, set the error flag and let the kernel return,
+ * leaving the context usable.  *error receives the device error word (1
+ * expected), *returned 1 if the waiting thread got past the wait, *wait_ok
+ * the wait's result (0 expected).  Synchronises the device; returns 0, or -1
+ * if a CUDA call failed. */
+int bgemm_debug_bounded_wait_selftest(unsigned long long limit_ns, int* error, int* returned,
+                                      int* wait_ok);
+
 #ifdef __cplusplus
 }
 #endif

@@ -254,3 +254,19 @@ def test_skewed_full_size_error_vs_fp64(cuda, mode):
     print("%s: max %.3g mean %.3g | simt max %.3g mean %.3g" % (mode, emax, emean, smax, smean))
     if mode == "tf32x3":
         assert emean <= 1.5 * smean
+
+
+def test_bounded_wait_expires_and_context_survives(cuda):
+    """A device-side wait on a barrier that nothing completes gives up after
+    its limit, raises the error word and returns; the context stays usable
+    (the failure path of every tensor-core kernel, without a GPU fault)."""
+    import ctypes
+    L = bg.lib()
+    L.bgemm_debug_bounded_wait_selftest.argtypes = [ctypes.c_ulonglong] + \
+        [ctypes.POINTER(ctypes.c_int)] * 3
+    err, ret, ok = ctypes.c_int(-1), ctypes.c_int(-1), ctypes.c_int(-1)
+    rc = L.bgemm_debug_bounded_wait_selftest(2_000_000, ctypes.byref(err), ctypes.byref(ret),
+                                             ctypes.byref(ok))
+    assert rc == 0
+    assert (err.value, ret.value, ok.value) == (1, 1, 0)
+    run_mode("tf32x3", [64, 200], [64, 100], [64, 300], 1.0, 0.0, seed=3)
