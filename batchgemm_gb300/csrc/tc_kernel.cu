@@ -125,7 +125,7 @@ __device__ __forceinline__ void put4(char* hi, char* lo, long long idx, const fl
 }
 
 // k per chunk of the pre-pass: each thread keeps kPackK / 8 loads in flight.
-constexpr int kPackK = 128;
+constexpr int kPackK = 256;
 
 // One job = 32 packed rows of one operand, walked in chunks of kPackK k.  Each
 // thread issues all kPackK / 8 of its loads for a chunk before it stores, and
