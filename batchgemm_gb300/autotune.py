@@ -40,7 +40,7 @@ def tc_dims(cfg):
 
 def valid_tc(mode, cfg):
     if cfg >= 8:
-        return mode != "tf32" and (cfg & 3) != 3
+        return (cfg & 3) != 3
     return True
 
 

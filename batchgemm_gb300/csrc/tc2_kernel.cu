@@ -37,11 +37,18 @@ namespace {
 constexpr int kRows = 128;                 // A-side rows per CTA
 constexpr int kA = kRows * 128;            // 16 KB per part
 constexpr int kB = 128 * 128;              // B-side half: up to 128 rows
-constexpr int kStage = 2 * (kA + kB);      // hi + lo of both sides: 64 KB
-constexpr int kS = 3;
-constexpr int kNAcc = 2;                   // 256-column group buffers
-constexpr int kNBar = 2 * kS + 2 * kNAcc + 1;
-constexpr int kSmem = kS * kStage + kNBar * 8 + 16 + 1024;
+constexpr int kNAcc = 2;                   // 256-column accumulator buffers
+// Stage ring: split modes hold hi + lo of both sides (64 KB, 3 stages), the
+// single-product TF32 mode hi only (32 KB, 6 stages).
+template <int SPLIT>
+struct Geo2 {
+  static constexpr int NP = SPLIT ? 2 : 1;
+  static constexpr int STAGE = NP * (kA + kB);
+  static constexpr int S = SPLIT ? 3 : 6;
+  static constexpr int NBAR = 2 * S + 2 * kNAcc + 1;
+  static constexpr int SMEM = S * STAGE + NBAR * 8 + 16 + 1024;
+};
+constexpr int kSmemMax = Geo2<1>::SMEM > Geo2<0>::SMEM ? Geo2<1>::SMEM : Geo2<0>::SMEM;
 constexpr int kEpiWarps2 = 8;              // 2 per TMEM lane quadrant
 constexpr int kCols = 128;                 // accumulator columns per epilogue warp
 constexpr int kThreads2 = 64 + kEpiWarps2 * 32;
@@ -61,8 +68,12 @@ __device__ __forceinline__ uint32_t make_idesc_pair(int n) {
          ((uint32_t)(256 >> 4) << 24);
 }
 
-template <int KIND>
+template <int KIND, int SPLIT>
 __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmParams p) {
+  using G = Geo2<SPLIT>;
+  constexpr int kS = G::S;
+  constexpr int kStage = G::STAGE;
+  constexpr int kNBar = G::NBAR;
   constexpr int KE = (KIND == kKindTF32) ? 32 : 64;  // elements per 128-byte slice
   constexpr int NSUB = 4;
   extern __shared__ uint8_t smem_raw[];
@@ -134,7 +145,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
           last_mat = ti.mat;
         }
         const int nk = (d.K + KE - 1) / KE;
-        const uint32_t tx = 2u * 2u * (uint32_t)(kA + hb * 128);  // both CTAs, hi + lo
+        const uint32_t tx = 2u * G::NP * (uint32_t)(kA + hb * 128);  // both CTAs, all parts
         const int row_a = ti.tm * 256 + (int)rank * kRows;
         const int row_b = ti.tn * bn + (int)rank * hb;
         for (int kb = 0; kb < nk; ++kb) {
@@ -143,7 +154,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
             break;
           }
           const uint32_t sa = sbase + st.idx * kStage;
-          const uint32_t sb = sa + 2 * kA;
+          const uint32_t sb = sa + G::NP * kA;
           const uint32_t fb = mapa_shared(full(st.idx), 0);
           if (leader) {
             mbar_arrive_expect_tx(full(st.idx), tx);
@@ -151,9 +162,11 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
             inflight_phase[st.idx] = st.phase;
           }
           tma_load_2d_pair(sa, tm + 0, kb * KE, row_a, fb);
-          tma_load_2d_pair(sa + kA, tm + 1, kb * KE, row_a, fb);
           tma_load_2d_pair(sb, tm + 2, kb * KE, row_b, fb);
-          tma_load_2d_pair(sb + kB, tm + 3, kb * KE, row_b, fb);
+          if (SPLIT) {
+            tma_load_2d_pair(sa + kA, tm + 1, kb * KE, row_a, fb);
+            tma_load_2d_pair(sb + kB, tm + 3, kb * KE, row_b, fb);
+          }
           st.next(kS);
         }
       }
@@ -185,7 +198,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
         const uint32_t idesc = make_idesc_pair<KIND>(bn);
         const int nk = (d.K + KE - 1) / KE;
         const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
-        const bool fine = d.K <= kFineK2;
+        const bool fine = SPLIT && d.K <= kFineK2;
         for (int kb = 0; kb < nk; ++kb) {
           if (!wait_bounded(full(st.idx), st.phase, p.error, abort, p.timeout_ns)) {
             ok = false;
@@ -193,9 +206,27 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
           }
           tc_fence_after();
           const uint32_t sa = sbase + st.idx * kStage;
-          const uint32_t sb = sa + 2 * kA;
+          const uint32_t sb = sa + G::NP * kA;
           const int s_end = min(NSUB, nsub - kb * NSUB);
-          if (fine) {
+          if (!SPLIT) {
+            // one product: a single accumulator per tile, the 2-deep ring
+            // alternating between tiles
+            if (kb == 0) {
+              if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
+                ok = false;
+                break;
+              }
+              tc_fence_after();
+            }
+            const uint32_t buf = tmem + acc.idx * 256u;
+            for (int s = 0; s < s_end; ++s)
+              mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc,
+                             (kb > 0 || s > 0) ? 1u : 0u);
+            if (kb == nk - 1) {
+              mma_commit_pair(tfull(acc.idx));
+              acc.next(kNAcc);
+            }
+          } else if (fine) {
             for (int s = 0; s < s_end && ok; ++s) {
               if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
                 ok = false;
@@ -267,7 +298,8 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       if (beta != 0.0f) c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
       const int nk = (d.K + KE - 1) / KE;
       const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
-      const int ngroups = (d.K <= kFineK2) ? nsub : (nk + kGroupKB2 - 1) / kGroupKB2;
+      const int ngroups = !SPLIT ? (nk > 0 ? 1 : 0)
+                          : (d.K <= kFineK2) ? nsub : (nk + kGroupKB2 - 1) / kGroupKB2;
       float r[kCols];
 #pragma unroll
       for (int j = 0; j < kCols; ++j) r[j] = 0.0f;
@@ -309,19 +341,20 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
   if (warp == 1) tmem_dealloc_pair(tmem, 512);
 }
 
-template <int KIND>
+template <int KIND, int SPLIT>
 cudaError_t launch2(const TcGemmParams& p, int grid, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc2_gemm_kernel<KIND>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+    cudaError_t e = cudaFuncSetAttribute(tc2_gemm_kernel<KIND, SPLIT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         Geo2<SPLIT>::SMEM);
     if (e != cudaSuccess) return e;
     attr = true;
   }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid, 1, 1);
   cfg.blockDim = dim3(kThreads2, 1, 1);
-  cfg.dynamicSmemBytes = kSmem;
+  cfg.dynamicSmemBytes = Geo2<SPLIT>::SMEM;
   cfg.stream = s;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -330,15 +363,18 @@ cudaError_t launch2(const TcGemmParams& p, int grid, cudaStream_t s) {
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, tc2_gemm_kernel<KIND>, p);
+  return cudaLaunchKernelEx(&cfg, tc2_gemm_kernel<KIND, SPLIT>, p);
 }
 
 }  // namespace
 
-cudaError_t tc2_gemm_launch(int kind, const TcGemmParams& p, int grid, cudaStream_t s) {
+cudaError_t tc2_gemm_launch(int kind, int split, const TcGemmParams& p, int grid,
+                            cudaStream_t s) {
   if (grid < 2 || (grid & 1)) return cudaErrorInvalidValue;
-  if (kind == kKindTF32) return launch2<kKindTF32>(p, grid, s);
-  return launch2<kKindBF16>(p, grid, s);
+  if (kind == kKindTF32 && !split) return launch2<kKindTF32, 0>(p, grid, s);
+  if (kind == kKindTF32) return launch2<kKindTF32, 1>(p, grid, s);
+  if (kind == kKindBF16 && split) return launch2<kKindBF16, 1>(p, grid, s);
+  return cudaErrorInvalidValue;
 }
 
 int tc2_max_clusters() {
@@ -346,7 +382,7 @@ int tc2_max_clusters() {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(2, 1, 1);
   cfg.blockDim = dim3(kThreads2, 1, 1);
-  cfg.dynamicSmemBytes = kSmem;
+  cfg.dynamicSmemBytes = kSmemMax;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = 2;
@@ -354,9 +390,9 @@ int tc2_max_clusters() {
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaFuncSetAttribute(tc2_gemm_kernel<kKindTF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       kSmem);
-  if (cudaOccupancyMaxActiveClusters(&n, tc2_gemm_kernel<kKindTF32>, &cfg) != cudaSuccess)
+  cudaFuncSetAttribute(tc2_gemm_kernel<kKindTF32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       kSmemMax);
+  if (cudaOccupancyMaxActiveClusters(&n, tc2_gemm_kernel<kKindTF32, 1>, &cfg) != cudaSuccess)
     return 0;
   return n;
 }

@@ -26,6 +26,7 @@ __host__ __device__ constexpr int tc_cfg_bn(int cfg) { return 16 << (cfg & 3); }
 __host__ __device__ constexpr bool tc_cfg_swap(int cfg) { return (cfg & 4) != 0; }
 // CTA-pair configurations (ids 8..15): a 256 x BN tile on two SMs,
 // BN = 64, 128, 256 (ids with (cfg & 3) == 3 are unused); bit 2 swaps.
+// Every mode can run them (tc2_kernel.cu).
 constexpr int kTcPairCfg0 = 8;
 __host__ __device__ constexpr bool tc_cfg_pair(int cfg) { return cfg >= kTcPairCfg0; }
 __host__ __device__ constexpr int tc2_cfg_bn(int cfg) { return 64 << (cfg & 3); }
@@ -103,8 +104,9 @@ cudaError_t tc_wait_selftest_launch(int* err, int* out, unsigned long long limit
 cudaError_t tc_tmap_launch(const TcTmapParams& p, cudaStream_t s);
 cudaError_t tc_gemm_launch(int kind, int split, const TcGemmParams& p, int grid, cudaStream_t s);
 int tc_smem_bytes(int kind, int split);
-// CTA-pair kernel (split modes); grid = 2 x clusters
-cudaError_t tc2_gemm_launch(int kind, const TcGemmParams& p, int grid, cudaStream_t s);
+// CTA-pair kernel; grid = 2 x clusters
+cudaError_t tc2_gemm_launch(int kind, int split, const TcGemmParams& p, int grid,
+                            cudaStream_t s);
 int tc2_max_clusters();
 // CTA-pair 3xTF32 kernel that splits raw FP32 operands in shared memory
 cudaError_t tc2s_gemm_launch(const TcGemmParams& p, int grid, cudaStream_t s);

@@ -55,8 +55,14 @@ static bool g_pair = false;
 static bool tc_eval(int c, int M, int N, int K, long long* tiles, double* t_tile) {
   if (tc_cfg_pair(c) != g_pair) return false;
   if (g_pair && !tc2_cfg_valid(c)) return false;
-  const TileCost& tc = kTcCost[g_mode - 1][c];
-  if (tc.b_ns <= 0.0f) return false;
+  TileCost tc = kTcCost[g_mode - 1][c];
+  if (tc.b_ns <= 0.0f) {
+    // not in the table (not yet tuned): the 3xTF32 cost of the same tile,
+    // halved per unit of K for a mode that loads and multiplies one part
+    const TileCost& t3 = kTcCost[BGEMM_MODE_TF32X3 - 1][c];
+    if (t3.b_ns <= 0.0f) return false;
+    tc = TileCost{t3.a_ns, g_mode == BGEMM_MODE_TF32X3 ? t3.b_ns : 0.5f * t3.b_ns};
+  }
   const bool swap = tc_cfg_swap(c);
   const int bm = g_pair ? 256 : kTcBM;
   const int bn = g_pair ? tc2_cfg_bn(c) : tc_cfg_bn(c);
@@ -86,9 +92,7 @@ bgemm_status_t tc_init(bgemm_plan_s* p, const bgemm_plan_options_t* opt) {
                        opt->force_tile_config, forced, fam);
     fam = forced;
   }
-  if (fam == 2 && !t->split_mode)
-    return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1, "CTA-pair tiles serve the split modes only");
-  if (t->split_mode) t->clusters = t->raw_ok ? tc2s_max_clusters() : tc2_max_clusters();
+  t->clusters = t->raw_ok ? tc2s_max_clusters() : tc2_max_clusters();
   if (fam == 2 && t->clusters < 1)
     return set_error(BGEMM_ERROR_NOT_SUPPORTED, 11, -1, "no CTA pair fits on this device");
   t->want_family = fam;
@@ -109,7 +113,7 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
                         opt, mp);
   }
   int fam = t->want_family;
-  if (fam == 0 && (!t->split_mode || t->clusters < 1)) fam = 1;
+  if (fam == 0 && t->clusters < 1) fam = 1;
   bgemm_status_t st = BGEMM_SUCCESS;
   if (fam == 0) {
     // plan both kernels with the cost table and keep the shorter makespan
@@ -389,7 +393,7 @@ bgemm_status_t tc_execute(bgemm_plan_s* p, float alpha, const float* const* dA,
                   p->d_counters, t->d_tmaps, alpha, beta, dC, t->d_err, 2000000000ull};
   if (p->ev_start) cudaEventRecord(p->ev_start, stream);
   e = t->raw    ? tc2s_gemm_launch(gp, p->grid, stream)
-      : t->pair ? tc2_gemm_launch(t->kind, gp, p->grid, stream)
+      : t->pair ? tc2_gemm_launch(t->kind, t->split, gp, p->grid, stream)
                 : tc_gemm_launch(t->kind, t->split, gp, p->grid, stream);
   if (p->ev_stop) cudaEventRecord(p->ev_stop, stream);
   if (e != cudaSuccess) return cuda_error(e, "tcgen05 GEMM launch");

@@ -155,8 +155,7 @@ def test_every_tile_config(cuda, cfg):
     K = rng.integers(1, 200, 10).tolist()
     for mode in ("tf32x3", "bf16x3"):
         run_mode(mode, M, N, K, 1.0, 0.25, force=cfg, seed=cfg)
-    if cfg < 8:
-        run_mode("tf32", M, N, K, 0.5, 0.0, force=cfg, seed=cfg)
+    run_mode("tf32", M, N, K, 0.5, 0.0, force=cfg, seed=cfg)
 
 
 @pytest.mark.parametrize("cfg", [8, 9, 10, 12, 13, 14, -1])
@@ -178,9 +177,15 @@ def test_split_in_kernel_variant(cuda, cfg):
     split_check(db, host, got, 0.5, 0.25, oracle.MODE_TF32X3, 16.0)
 
 
-def test_pair_tiles_rejected_for_single_product(cuda):
-    with pytest.raises(bg.BgemmError):
-        bg.Plan([300], [300], [300], [300], [300], [300], mode="tf32", force_tile_config=9)
+def test_pair_tiles_for_single_product(cuda):
+    """The single-product TF32 mode runs on CTA pairs too (hi panels only,
+    one accumulator per tile), including K = 0 and ragged edges."""
+    M, N, K = [300, 1024, 17, 5], [300, 700, 1, 900], [300, 1024, 0, 77]
+    for cfg in (8, 9, 10, 12, 13, 14):
+        with bg.Plan(M, N, K, M, [max(1, k) for k in K], M, mode="tf32",
+                     force_tile_config=cfg) as p:
+            assert sum(p.info()["tile_config_hist"][8:]) == 4
+        run_mode("tf32", M, N, K, 1.0, 0.5, force=cfg, seed=cfg)
 
 
 def test_pair_mode_chosen_for_large_matrices(cuda):
