@@ -8,7 +8,8 @@ The C restatement lives in ``oracle.c`` (semantics and reference citations in
 its header).  ``build()`` compiles it with gcc into ``oracle/_build``;
 ``build_ref_emul()`` compiles the reference's own tile bodies into
 ``oracle/_ref/ref_emul`` when the reference checkout is present (golden-vector
-generation only).
+generation only); ``build_ref_gpu()`` compiles the reference's GPU kernels
+unchanged into ``oracle/_ref/ref_framework.cubin`` (GPU parity and timing).
 """
 from __future__ import annotations
 
@@ -52,6 +53,16 @@ def build_ref_emul(ref_root: str = "/root/reference") -> Optional[str]:
     subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref_emul"), "REF=" + ref_root,
                     "OUT=" + REF_DIR], check=True)
     return os.path.join(REF_DIR, "ref_emul")
+
+
+def build_ref_gpu(ref_root: str = "/root/reference") -> Optional[str]:
+    """Build the reference framework kernels' cubin (only where the reference
+    exists); returns its path, or the prebuilt one, or None."""
+    out = os.path.join(REF_DIR, "ref_framework.cubin")
+    if os.path.isdir(os.path.join(ref_root, "CUDA", "framework")):
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref_gpu"), "REF=" + ref_root,
+                        "OUT=" + REF_DIR], check=True)
+    return out if os.path.exists(out) else None
 
 
 def lib() -> ctypes.CDLL:

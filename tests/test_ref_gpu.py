@@ -1,0 +1,146 @@
+"""The reference framework's own GPU kernel on the GB300, beside the drop-in.
+
+oracle/_ref/ref_framework.cubin is the reference's CUDA/framework/kernel.h
+compiled unchanged for sm_103a (oracle/ref_gpu/).  The test loads it with the
+driver API and launches the reference's `gemm` kernel (kernel.h:11) the way
+the reference's host code does (gemm.cu:181-200: a dense grid of
+(max tiles along M, max tiles along N, batch) blocks, 16 KB of dynamic shared
+memory), every matrix on the reference's column-major tile strategy 2
+(32 x 32, kernel_128_new.h:131).  The other strategies mix row- and
+column-major indexing as shipped, so they are not run.  Strategy 2 needs M and
+N multiples of 32 and K a multiple of 8, and uses 128 of the block's threads:
+the launch gives it exactly 128 threads, so every thread reaches its barriers.
+
+The drop-in bgemm_framework_gemm must produce the same C, bit for bit, from
+the same device arrays (the GPU pin of the oracle's fma order), and the
+timings of both are printed (informational).
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+import batchgemm_gb300 as bg  # noqa: E402
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CUBIN = os.path.join(ROOT, "oracle", "_ref", "ref_framework.cubin")
+GEMM_SYMBOL = b"_Z4gemmPiS_S_PPfS1_S1_S_"  # gemm(int*, int*, int*, float**, float**, float**, int*)
+
+
+class RefKernel:
+    def __init__(self):
+        self.cu = ctypes.CDLL("libcuda.so.1")
+        self.mod = ctypes.c_void_p()
+        rc = self.cu.cuModuleLoad(ctypes.byref(self.mod), CUBIN.encode())
+        assert rc == 0, "cuModuleLoad: %d" % rc
+        self.fn = ctypes.c_void_p()
+        rc = self.cu.cuModuleGetFunction(ctypes.byref(self.fn), self.mod, GEMM_SYMBOL)
+        assert rc == 0, "cuModuleGetFunction: %d" % rc
+
+    def launch(self, grid, dM, dN, dK, dA, dB, dC, dT, stream=0):
+        args = [ctypes.c_void_p(x) for x in (dM, dN, dK, dA, dB, dC, dT)]
+        params = (ctypes.c_void_p * 7)(*[ctypes.cast(ctypes.pointer(a), ctypes.c_void_p)
+                                         for a in args])
+        rc = self.cu.cuLaunchKernel(self.fn, ctypes.c_uint(grid[0]), ctypes.c_uint(grid[1]),
+                                    ctypes.c_uint(grid[2]), ctypes.c_uint(128), ctypes.c_uint(1),
+                                    ctypes.c_uint(1), ctypes.c_uint(4 * 4 * 128 * 8),
+                                    ctypes.c_void_p(stream), params, None)
+        assert rc == 0, "cuLaunchKernel: %d" % rc
+
+    def close(self):
+        self.cu.cuModuleUnload(self.mod)
+
+
+@pytest.fixture(scope="module")
+def ref_kernel(cuda):
+    if not os.path.exists(CUBIN):
+        pytest.skip("reference cubin not built (needs the reference checkout at build time)")
+    torch.zeros(1, device="cuda")  # the runtime's primary context is current
+    k = RefKernel()
+    yield k
+    k.close()
+
+
+def batch_arrays(M, N, K, seed):
+    rng = np.random.default_rng(seed)
+    dev = "cuda"
+    bufs = {}
+    for name, rows, cols in (("A", M, K), ("B", K, N), ("C", M, N)):
+        sizes = [r * c for r, c in zip(rows, cols)]
+        offs = np.concatenate([[0], np.cumsum([(s + 3) // 4 * 4 for s in sizes])[:-1]]).astype(int)
+        host = rng.uniform(-1, 1, int(offs[-1] + sizes[-1] + 4)).astype(np.float32)
+        buf = torch.from_numpy(host).to(dev)
+        ptrs = torch.tensor([buf.data_ptr() + 4 * int(o) for o in offs], dtype=torch.int64,
+                            device=dev)
+        bufs[name] = (buf, ptrs)
+    ints = {k: torch.tensor(v, dtype=torch.int32, device=dev) for k, v in
+            (("M", M), ("N", N), ("K", K), ("T", [2] * len(M)))}
+    return bufs, ints
+
+
+def shapes(seed, n):
+    rng = np.random.default_rng(seed)
+    M = (rng.integers(1, 17, n) * 32).tolist()
+    N = (rng.integers(1, 17, n) * 32).tolist()
+    K = (rng.integers(1, 65, n) * 8).tolist()
+    return M, N, K
+
+
+def run_both(ref, M, N, K, seed):
+    bufs, ints = batch_arrays(M, N, K, seed)
+    C0 = bufs["C"][0].clone()
+    grid = (max(m // 32 for m in M), max(n // 32 for n in N), len(M))
+    ref.launch(grid, ints["M"].data_ptr(), ints["N"].data_ptr(), ints["K"].data_ptr(),
+               bufs["A"][1].data_ptr(), bufs["B"][1].data_ptr(), bufs["C"][1].data_ptr(),
+               ints["T"].data_ptr())
+    torch.cuda.synchronize()
+    c_ref = bufs["C"][0].clone()
+    bufs["C"][0].copy_(C0)
+    bg.framework_gemm(ints["M"].data_ptr(), ints["N"].data_ptr(), ints["K"].data_ptr(),
+                      bufs["A"][1].data_ptr(), bufs["B"][1].data_ptr(), bufs["C"][1].data_ptr(),
+                      len(M), max(max(M), max(N)))
+    torch.cuda.synchronize()
+    bg.framework_check_device()
+    return c_ref, bufs["C"][0].clone(), bufs, ints, grid, C0
+
+
+def test_reference_kernel_matches_drop_in_bit_for_bit(ref_kernel):
+    for seed, n in ((1, 8), (2, 64), (3, 256)):
+        M, N, K = shapes(seed, n)
+        c_ref, c_ours, *_ = run_both(ref_kernel, M, N, K, seed)
+        a = c_ref.cpu().numpy().view(np.uint32)
+        b = c_ours.cpu().numpy().view(np.uint32)
+        bad = np.nonzero(a != b)[0]
+        assert bad.size == 0, "batch %d: %d words differ" % (n, bad.size)
+
+
+def test_reference_kernel_timing(ref_kernel):
+    """Informational: the reference's dense-grid kernel vs the persistent
+    drop-in on the same arrays (printed, not asserted)."""
+    M, N, K = shapes(5, 2048)
+    _, _, bufs, ints, grid, _ = run_both(ref_kernel, M, N, K, 5)
+    flops = sum(2.0 * m * n * k for m, n, k in zip(M, N, K))
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    reps = 10
+    e[0].record()
+    for _ in range(reps):
+        ref_kernel.launch(grid, ints["M"].data_ptr(), ints["N"].data_ptr(), ints["K"].data_ptr(),
+                          bufs["A"][1].data_ptr(), bufs["B"][1].data_ptr(),
+                          bufs["C"][1].data_ptr(), ints["T"].data_ptr())
+    e[1].record()
+    e[2].record()
+    for _ in range(reps):
+        bg.framework_gemm(ints["M"].data_ptr(), ints["N"].data_ptr(), ints["K"].data_ptr(),
+                          bufs["A"][1].data_ptr(), bufs["B"][1].data_ptr(),
+                          bufs["C"][1].data_ptr(), len(M), max(max(M), max(N)))
+    e[3].record()
+    torch.cuda.synchronize()
+    t_ref = e[0].elapsed_time(e[1]) / reps
+    t_ours = e[2].elapsed_time(e[3]) / reps
+    print("\nreference gemm (strategy 2): %.3f ms = %.2f TFLOP/s; drop-in: %.3f ms = %.2f TFLOP/s"
+          % (t_ref, flops / t_ref / 1e9, t_ours, flops / t_ours / 1e9))
