@@ -97,7 +97,8 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+        import tempfile
+        self.path = os.path.join(tempfile.gettempdir(), "bgemm_clocks_%d.csv" % os.getpid())
 
     def __enter__(self):
         try:
