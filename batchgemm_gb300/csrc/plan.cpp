@@ -275,6 +275,54 @@ int debug_simt_queue(const int* M, const int* N, const int* K, int batch, int sl
   return (int)n;
 }
 
+static bgemm_status_t plan_batch(bgemm_plan_s* p, const int* M, const int* N, const int* K,
+                                 const int* lda, const int* ldb, const int* ldc, int batch,
+                                 bool first, BatchPlan& bp);
+static bgemm_plan_options_t default_options();
+
+// Host-only replay of the tensor-core planner with a given number of one-SM
+// slots and CTA pairs (tests; no GPU needed).  Returns the number of items,
+// or -1 on error / overflow.
+int debug_tc_plan(const int* M, const int* N, const int* K, int batch, int mode, int family,
+                  int slots, int clusters, int* cfg_out, int* items_out, int max_items,
+                  long long* ws_out, int* jobs_out, int max_jobs, int* n_jobs,
+                  long long* ws_bytes, int* pair) {
+  if (mode < BGEMM_MODE_TF32 || mode > BGEMM_MODE_BF16X3 || slots < 1 || clusters < 0) return -1;
+  std::vector<int> ld(batch);
+  for (int i = 0; i < batch; ++i) ld[i] = std::max(1, std::max(M[i], K[i]));
+  bgemm_plan_s p;
+  p.mode = mode;
+  p.facts = DeviceFacts{0, 103, slots, 2, 1};
+  p.opt = default_options();
+  p.opt.kernel_family = family;
+  BatchPlan bp;
+  bgemm_status_t st = tc_init(&p, &p.opt, clusters);
+  if (st == BGEMM_SUCCESS)
+    st = plan_batch(&p, M, N, K, ld.data(), ld.data(), ld.data(), batch, true, bp);
+  int n = -1;
+  if (st == BGEMM_SUCCESS) {
+    n = bp.req.tiles;
+    for (int i = 0; cfg_out && i < batch; ++i)
+      cfg_out[i] = (M[i] && N[i]) ? bp.descs[i].cfg | (bp.descs[i].aux & kTcSwapFlag ? 1 << 8 : 0)
+                                  : -1;
+    if (items_out) {
+      if (n > max_items) {
+        n = -1;
+      } else {
+        for (int t = 0; t < n; ++t) {
+          items_out[3 * t] = bp.items[t].mat;
+          items_out[3 * t + 1] = bp.items[t].tm;
+          items_out[3 * t + 2] = bp.items[t].tn;
+        }
+      }
+    }
+    tc_debug_layout(&p, ws_out, jobs_out, max_jobs, n_jobs, pair);
+    *ws_bytes = (long long)bp.req.workspace_bytes;
+  }
+  if (p.tc) tc_plan_release(&p);
+  return n;
+}
+
 static void free_plan_memory(bgemm_plan_s* p) {
   if (p->d_mem) cudaFree(p->d_mem);
   for (int s = 0; s < 2; ++s) {
@@ -856,6 +904,19 @@ int bgemm_debug_compare_tensor_maps(void* plan, void* stream, int* n_maps, int* 
   if (!plan || !n_maps || !n_diff || !first_byte) return -1;
   return tc_debug_compare_tmaps(static_cast<bgemm_plan_s*>(plan),
                                 static_cast<cudaStream_t>(stream), n_maps, n_diff, first_byte);
+}
+
+int bgemm_debug_tc_plan(const int* M, const int* N, const int* K, int batch, int mode,
+                        int family, int slots, int clusters, int* cfg_out, int* items_out,
+                        int max_items, long long* ws_out, int* jobs_out, int max_jobs,
+                        int* n_jobs, long long* ws_bytes, int* kernel_family) {
+  clear_error();
+  if (batch < 0 || (batch > 0 && (!M || !N || !K)) || !n_jobs || !ws_bytes || !kernel_family)
+    return -1;
+  for (int i = 0; i < batch; ++i)
+    if (M[i] < 0 || N[i] < 0 || K[i] < 0) return -1;
+  return debug_tc_plan(M, N, K, batch, mode, family, slots, clusters, cfg_out, items_out,
+                       max_items, ws_out, jobs_out, max_jobs, n_jobs, ws_bytes, kernel_family);
 }
 
 int bgemm_debug_simt_queue(const int* M, const int* N, const int* K, int batch, int slots,

@@ -98,7 +98,10 @@ bgemm_status_t choose_tiles(int ncfg, TileEval eval, const int* M, const int* N,
 
 // tensor-core hooks (tc_plan.cpp)
 // tc_init: mode facts and option checks, once per plan.
-bgemm_status_t tc_init(bgemm_plan_s* p, const bgemm_plan_options_t* opt);
+// clusters >= 0 overrides the CTA pairs the device fits (host-only replays).
+bgemm_status_t tc_init(bgemm_plan_s* p, const bgemm_plan_options_t* opt, int clusters = -1);
+void tc_debug_layout(bgemm_plan_s* p, long long* ws_out, int* jobs_out, int max_jobs,
+                     int* n_jobs, int* pair);
 // tc_choose: tile configurations of a batch; the first call of a plan also
 // fixes its kernel family (one-SM or CTA pair), later calls keep it.
 bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int* K, int batch,

@@ -73,7 +73,7 @@ static bool tc_eval(int c, int M, int N, int K, long long* tiles, double* t_tile
   return true;
 }
 
-bgemm_status_t tc_init(bgemm_plan_s* p, const bgemm_plan_options_t* opt) {
+bgemm_status_t tc_init(bgemm_plan_s* p, const bgemm_plan_options_t* opt, int clusters) {
   auto* t = new TcPlan();
   p->tc = t;
   t->kind = (p->mode == BGEMM_MODE_BF16X3) ? kKindBF16 : kKindTF32;
@@ -92,7 +92,7 @@ bgemm_status_t tc_init(bgemm_plan_s* p, const bgemm_plan_options_t* opt) {
                        opt->force_tile_config, forced, fam);
     fam = forced;
   }
-  t->clusters = t->raw_ok ? tc2s_max_clusters() : tc2_max_clusters();
+  t->clusters = clusters >= 0 ? clusters : t->raw_ok ? tc2s_max_clusters() : tc2_max_clusters();
   if (fam == 2 && t->clusters < 1)
     return set_error(BGEMM_ERROR_NOT_SUPPORTED, 11, -1, "no CTA pair fits on this device");
   t->want_family = fam;
@@ -424,6 +424,26 @@ void tc_plan_release(bgemm_plan_s* p) {
   p->tc = nullptr;
 }
 
+}  // namespace bgemm
+
+namespace bgemm {
+// The pre-pass layout of the last planned batch (host-only debug replay).
+void tc_debug_layout(bgemm_plan_s* p, long long* ws_out, int* jobs_out, int max_jobs,
+                     int* n_jobs, int* pair) {
+  TcPlan* t = p->tc;
+  for (size_t i = 0; ws_out && i < t->pd.size(); ++i) {
+    const PackDesc& q = t->pd[i];
+    const long long v[5] = {q.a_hi, q.a_lo, q.b_hi, q.b_lo, q.kpad};
+    for (int k = 0; k < 5; ++k) ws_out[5 * i + k] = v[k];
+  }
+  *n_jobs = (int)t->jobs.size();
+  for (int j = 0; jobs_out && j < *n_jobs && j < max_jobs; ++j) {
+    jobs_out[3 * j] = t->jobs[j].mat;
+    jobs_out[3 * j + 1] = t->jobs[j].op;
+    jobs_out[3 * j + 2] = t->jobs[j].r0;
+  }
+  *pair = t->pair ? 2 : 1;
+}
 }  // namespace bgemm
 
 extern "C" int bgemm_debug_bounded_wait_selftest(unsigned long long limit_ns, int* error,

@@ -25,6 +25,23 @@ int bgemm_debug_simt_queue(const int* M, const int* N, const int* K, int batch, 
                            int force_cfg, int rebalance, int* cfg_out, int* items_out,
                            int max_items);
 
+/* Host-only replay of the tensor-core planner for `mode` (1 TF32, 2 TF32X3,
+ * 3 BF16X3) as it would plan on a device with `slots` one-SM persistent CTAs
+ * and `clusters` CTA pairs (family: 0 cost model, 1 one-SM tiles, 2 CTA
+ * pairs).  Every output may be NULL.  cfg_out[batch]: tile configuration
+ * (bit 8 set when the operands are swapped, -1 for empty matrices);
+ * items_out[3*max_items]: (matrix, tile along the MMA's M side, tile along
+ * its N side) in queue order; ws_out[5*batch]: byte offsets of the packed
+ * A hi, A lo, B hi, B lo panels and the padded row length kpad (elements);
+ * jobs_out[3*max_jobs]: pre-pass strips (matrix, operand 0 A / 1 B, first
+ * row).  *n_jobs, *ws_bytes and *kernel_family (1 one-SM, 2 pairs) are
+ * always written.  Returns the number of work items, or -1 on invalid sizes,
+ * planner errors, or max_items too small. */
+int bgemm_debug_tc_plan(const int* M, const int* N, const int* K, int batch, int mode,
+                        int family, int slots, int clusters, int* cfg_out, int* items_out,
+                        int max_items, long long* ws_out, int* jobs_out, int max_jobs,
+                        int* n_jobs, long long* ws_bytes, int* kernel_family);
+
 /* Tensor-core plans: waits for `stream`, encodes on the host the tensor maps
  * that the device built for the plan, and compares them byte by byte.
  * *n_maps receives the number of maps compared, *n_diff how many differ,
