@@ -622,6 +622,11 @@ bgemm_status_t plan_execute(bgemm_plan_t p, float alpha, const float* const* dA,
   if (!dA) return set_error(BGEMM_ERROR_INVALID_VALUE, 3, -1, "dA is NULL");
   if (!dB) return set_error(BGEMM_ERROR_INVALID_VALUE, 4, -1, "dB is NULL");
   if (!dC) return set_error(BGEMM_ERROR_INVALID_VALUE, 6, -1, "dC is NULL");
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != p->facts.device)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan belongs to device %d, current is %d",
+                     p->facts.device, dev);
   if (p->row_major) std::swap(dA, dB);
   if (p->mode == BGEMM_MODE_SIMT_FP32) {
     SimtParams sp{p->d_descs, p->d_items,  p->n_items, p->d_counters + kHdrItems,
