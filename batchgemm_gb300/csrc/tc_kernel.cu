@@ -22,8 +22,9 @@
 // with truncation, so a long chain of MMAs into one accumulator drifts
 // toward zero (measured on GB300: -1.1e-7 of sum|ab| at K = 2048, against
 // 2e-8 unbiased for an FP32 fma chain).  The split modes therefore never let
-// a chain run long: every group of MMAs (32 k, or 8 k for matrices with
-// K <= 64) accumulates into a fresh buffer of a 4-deep TMEM ring -- the
+// a chain run long: every group of MMAs (two 128-byte K slices, i.e. 64 k
+// for TF32, or one MMA for matrices with K <= 64, which also keep lo*lo)
+// accumulates into a fresh buffer of a 4-deep TMEM ring -- the
 // small hi*lo and lo*hi products first, hi*hi last -- and the epilogue warps
 // add each finished group into FP32 registers with round-to-nearest while
 // the MMAs of the next groups run.  The single-product TF32 mode keeps one
