@@ -156,6 +156,7 @@ def lib() -> ctypes.CDLL:
     L.bgemm_framework_gemm.argtypes = [vp, vp, vp, vp, vp, vp, vp, i, i, vp]
     L.bgemm_framework_check_device.argtypes = [vp]
     L.bgemm_framework_gemm_noalloc.argtypes = [vp, vp, vp, vp, vp, vp, i, i, vp, vp]
+    L.bgemm_framework_gemm_mode.argtypes = [vp, vp, vp, vp, vp, vp, i, i, i, i, vp]
     L.bgemm_last_error_arg.argtypes = [ip]
     L.bgemm_last_error_arg.restype = i
     L.bgemm_last_error_message.restype = ctypes.c_char_p
@@ -166,7 +167,7 @@ def lib() -> ctypes.CDLL:
     for name in ("bgemm_sgemm_vbatched", "bgemm_plan_create", "bgemm_plan_create_ex",
                  "bgemm_plan_execute", "bgemm_plan_info", "bgemm_plan_check_device",
                  "bgemm_plan_destroy", "bgemm_framework_gemm", "bgemm_framework_check_device",
-                 "bgemm_framework_gemm_noalloc", "bgemm_device_info",
+                 "bgemm_framework_gemm_noalloc", "bgemm_framework_gemm_mode", "bgemm_device_info",
                  "bgemm_plan_set_kernel_events", "bgemm_plan_requirements",
                  "bgemm_plan_update", "bgemm_plan_capacity", "bgemm_sgemm_vbatched_ex"):
         getattr(L, name).restype = i
@@ -314,6 +315,15 @@ def framework_gemm(dM, dN, dK, dA, dB, dC, batch: int, max_dim: int, stream=None
     """Reference drop-in: device size arrays, C_i += A_i B_i (lda=M, ldb=K, ldc=M)."""
     _check(lib().bgemm_framework_gemm(dM, dN, dK, dA, dB, dC, dT, int(batch), int(max_dim),
                                       _stream(stream)))
+
+
+def framework_gemm_mode(dM, dN, dK, dA, dB, dC, batch: int, max_dim: int, max_k: int,
+                        mode="tf32x3", stream=None) -> None:
+    """The same device-size entry in any mode: for the tensor-core modes the
+    tile queue, split operands and tensor maps are built on the device.
+    max_dim bounds every M and N, max_k every K (they size the scratch)."""
+    _check(lib().bgemm_framework_gemm_mode(dM, dN, dK, dA, dB, dC, int(batch), int(max_dim),
+                                           int(max_k), _mode(mode), _stream(stream)))
 
 
 def framework_check_device(stream=None) -> None:

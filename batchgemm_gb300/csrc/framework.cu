@@ -244,6 +244,8 @@ extern "C" bgemm_status_t bgemm_framework_check_device(bgemm_stream_t stream) {
   cudaGetDevice(&dev);
   cudaError_t e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) return cuda_error(e, "cudaStreamSynchronize");
+  bgemm_status_t st = fwtc_check_device(dev);
+  if (st != BGEMM_SUCCESS) return st;
   std::lock_guard<std::mutex> lk(g_fw_mu);
   auto it = g_fw.find(dev);
   if (it == g_fw.end() || !it->second.mem) return BGEMM_SUCCESS;

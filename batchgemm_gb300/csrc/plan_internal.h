@@ -122,5 +122,7 @@ bgemm_status_t tc_check_device(bgemm_plan_s* p, cudaStream_t stream);
 int tc_debug_compare_tmaps(bgemm_plan_s* p, cudaStream_t stream, int* n_maps, int* n_diff,
                            int* first_byte);
 void tc_plan_release(bgemm_plan_s* p);
+// errors of the device-resident tensor-core path (framework_tc.cu)
+bgemm_status_t fwtc_check_device(int dev);
 
 }  // namespace bgemm

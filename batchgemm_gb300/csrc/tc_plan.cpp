@@ -245,6 +245,21 @@ static bool encode_matrix_maps(const TcPlan* t, const MatDesc& d, const PackDesc
   return true;
 }
 
+// Templates per (box height, extent class); the device patches one copy per
+// operand panel (address, dims, row stride).
+bool tc_encode_templates(int kind, void* base, CUtensorMap* tpl) {
+  const int esz = (kind == kKindBF16) ? 2 : 4;
+  const int ke = 128 / esz;
+  for (int b = 16; b <= 128; b *= 2) {
+    if (!encode_panel(&tpl[tmap_template_index(b, false)], kind, base, ke, kTcBM, ke,
+                      b) ||  // 128 rows x 128 B = 16 KiB
+        !encode_panel(&tpl[tmap_template_index(b, true)], kind, base, ke, 1 << 20, ke,
+                      b))  // 2^20 rows x 128 B = 128 MiB
+      return false;
+  }
+  return true;
+}
+
 bgemm_status_t tc_alloc(bgemm_plan_s* p) {
   TcPlan* t = p->tc;
   t->cap_batch = p->cap.batch;
@@ -266,21 +281,8 @@ bgemm_status_t tc_alloc(bgemm_plan_s* p) {
     return set_error(BGEMM_ERROR_ALLOC, 0, -1, "tensor-core plan memory: %s",
                      cudaGetErrorString(e));
   for (int s = 0; s < 2; ++s) std::memset(t->h_stage[s], 0, t->mem_bytes);
-  {
-    // templates per (box height, extent class); the device patches one copy
-    // per operand panel (address, dims, row stride)
-    const int esz = (t->kind == kKindBF16) ? 2 : 4;
-    const int ke = 128 / esz;
-    auto* tpl = static_cast<CUtensorMap*>(t->h_stage[0]);
-    void* ws = t->d_ws;
-    for (int b = 16; b <= 128; b *= 2) {
-      const bool ok = encode_panel(&tpl[tmap_template_index(b, false)], t->kind, ws, ke, kTcBM, ke,
-                                   b) &&  // 128 rows x 128 B = 16 KiB
-                      encode_panel(&tpl[tmap_template_index(b, true)], t->kind, ws, ke, 1 << 20,
-                                   ke, b);  // 2^20 rows x 128 B = 128 MiB
-      if (!ok) return set_error(BGEMM_ERROR_INTERNAL, 0, -1, "template tensor map encoding failed");
-    }
-  }
+  if (!tc_encode_templates(t->kind, t->d_ws, static_cast<CUtensorMap*>(t->h_stage[0])))
+    return set_error(BGEMM_ERROR_INTERNAL, 0, -1, "template tensor map encoding failed");
   char* dm = static_cast<char*>(t->d_mem);
   t->d_templ = reinterpret_cast<CUtensorMap*>(dm);
   t->d_tmaps = reinterpret_cast<CUtensorMap*>(dm + t->off_tm);

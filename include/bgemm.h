@@ -249,6 +249,30 @@ bgemm_status_t bgemm_framework_gemm(const int* dM, const int* dN,
                                     bgemm_stream_t stream);
 bgemm_status_t bgemm_framework_check_device(bgemm_stream_t stream);
 
+/* --- the same entry in any mode ------------------------------------------
+ * No counterpart in the reference (its kernel is FP32 only).  Same arguments
+ * and result as bgemm_framework_gemm (device arrays of sizes and pointers,
+ * C_i += A_i*B_i, lda = M_i, ldb = K_i, ldc = M_i), in any bgemm_mode_t.  For
+ * the tensor-core modes the tile choice (CTA-pair tiles, the autotuned cost
+ * table), the tile queue, the split-operand layout, the pre-pass strips and
+ * the tensor maps are all built on the device, so the sizes never leave it
+ * and a captured sequence of calls replays with whatever the size arrays
+ * hold.  max_dim bounds every M_i and N_i, max_k every K_i: the library's
+ * scratch (about batch * 2 * max_dim * max_k * 8 bytes of split operands for
+ * TF32X3) is sized from them, and a matrix outside them is skipped and
+ * reported by bgemm_framework_check_device, which also reports an expired
+ * device wait (BGEMM_ERROR_DEVICE_TIMEOUT).  Calls in one mode on one device
+ * share that scratch, so order them (one stream, or events between streams);
+ * a call that grows it (the first, or larger batch / max_dim / max_k)
+ * allocates and must not be inside a stream capture.  BGEMM_MODE_SIMT_FP32 is exactly
+ * bgemm_framework_gemm (max_k unused).  Argument numbers: dM 1, dN 2, dK 3,
+ * dA 4, dB 5, dC 6, batch 7, max_dim 8, max_k 9, mode 10. */
+bgemm_status_t bgemm_framework_gemm_mode(const int* dM, const int* dN,
+                                         const int* dK, float* const* dA,
+                                         float* const* dB, float* const* dC,
+                                         int batch, int max_dim, int max_k,
+                                         bgemm_mode_t mode, bgemm_stream_t stream);
+
 /* --- allocation-free variant of bgemm_framework_gemm ----------------------
  * No counterpart in the reference.  Same arguments and result as
  * bgemm_framework_gemm (device size arrays, C_i += A_i*B_i, FP32 SIMT,
