@@ -13,8 +13,9 @@ import os
 from typing import Optional, Sequence
 
 __all__ = [
-    "BgemmError", "MODES", "lib", "build", "sgemm_vbatched", "Plan", "framework_gemm",
-    "framework_check_device", "device_info", "LIB_PATH",
+    "BgemmError", "MODES", "lib", "build", "sgemm_vbatched", "sgemm_vbatched_ex", "Plan",
+    "plan_requirements", "max_requirements", "framework_gemm", "framework_gemm_mode",
+    "framework_release", "framework_check_device", "device_info", "LIB_PATH",
 ]
 
 PKG = os.path.dirname(os.path.abspath(__file__))
@@ -155,8 +156,10 @@ def lib() -> ctypes.CDLL:
     L.bgemm_plan_destroy.argtypes = [vp]
     L.bgemm_framework_gemm.argtypes = [vp, vp, vp, vp, vp, vp, vp, i, i, vp]
     L.bgemm_framework_check_device.argtypes = [vp]
+    L.bgemm_framework_release.argtypes = []
     L.bgemm_framework_gemm_noalloc.argtypes = [vp, vp, vp, vp, vp, vp, i, i, vp, vp]
-    L.bgemm_framework_gemm_mode.argtypes = [vp, vp, vp, vp, vp, vp, i, i, i, i, vp]
+    L.bgemm_framework_gemm_mode.argtypes = [vp, vp, vp, vp, vp, vp, i, i, i, ctypes.c_longlong,
+                                            i, vp]
     L.bgemm_last_error_arg.argtypes = [ip]
     L.bgemm_last_error_arg.restype = i
     L.bgemm_last_error_message.restype = ctypes.c_char_p
@@ -167,7 +170,8 @@ def lib() -> ctypes.CDLL:
     for name in ("bgemm_sgemm_vbatched", "bgemm_plan_create", "bgemm_plan_create_ex",
                  "bgemm_plan_execute", "bgemm_plan_info", "bgemm_plan_check_device",
                  "bgemm_plan_destroy", "bgemm_framework_gemm", "bgemm_framework_check_device",
-                 "bgemm_framework_gemm_noalloc", "bgemm_framework_gemm_mode", "bgemm_device_info",
+                 "bgemm_framework_gemm_noalloc", "bgemm_framework_gemm_mode", "bgemm_framework_release",
+                 "bgemm_device_info",
                  "bgemm_plan_set_kernel_events", "bgemm_plan_requirements",
                  "bgemm_plan_update", "bgemm_plan_capacity", "bgemm_sgemm_vbatched_ex"):
         getattr(L, name).restype = i
@@ -318,12 +322,20 @@ def framework_gemm(dM, dN, dK, dA, dB, dC, batch: int, max_dim: int, stream=None
 
 
 def framework_gemm_mode(dM, dN, dK, dA, dB, dC, batch: int, max_dim: int, max_k: int,
-                        mode="tf32x3", stream=None) -> None:
+                        mode="tf32x3", stream=None, max_operand_elems: int = 0) -> None:
     """The same device-size entry in any mode: for the tensor-core modes the
     tile queue, split operands and tensor maps are built on the device.
-    max_dim bounds every M and N, max_k every K (they size the scratch)."""
+    max_dim bounds every M and N, max_k every K, max_operand_elems the sum of
+    (M + N) * K over the batch (0: batch * 2 * max_dim * max_k); they size
+    the library's scratch."""
     _check(lib().bgemm_framework_gemm_mode(dM, dN, dK, dA, dB, dC, int(batch), int(max_dim),
-                                           int(max_k), _mode(mode), _stream(stream)))
+                                           int(max_k), int(max_operand_elems), _mode(mode),
+                                           _stream(stream)))
+
+
+def framework_release() -> None:
+    """Free the framework entries' scratch on the current device."""
+    _check(lib().bgemm_framework_release())
 
 
 def framework_check_device(stream=None) -> None:

@@ -239,6 +239,23 @@ cudaError_t fw_launch_on_scratch(const int* dM, const int* dN, const int* dK, fl
 
 }  // namespace bgemm
 
+extern "C" bgemm_status_t bgemm_framework_release(void) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+  {
+    std::lock_guard<std::mutex> lk(g_fw_mu);
+    auto it = g_fw.find(dev);
+    if (it != g_fw.end() && it->second.mem) {
+      e = cudaFree(it->second.mem);  // waits for kernels still using it
+      it->second.mem = nullptr;
+      it->second.cap_batch = it->second.cap_items = 0;
+      if (e != cudaSuccess) return cuda_error(e, "framework scratch release");
+    }
+  }
+  return fwtc_release(dev);
+}
+
 extern "C" bgemm_status_t bgemm_framework_check_device(bgemm_stream_t stream) {
   int dev = 0;
   cudaGetDevice(&dev);

@@ -16,8 +16,8 @@
 //      CTA-pair GEMM run as for a plan, reading item and strip counts from
 //      the device.
 // Scratch (descriptors, queue, maps, workspace) is owned by the library, one
-// buffer per device and mode, sized from batch, max_dim and max_k and grown
-// when a call needs more.
+// buffer per device and mode, sized from batch, max_dim, max_k and the bound
+// on the batch's operand elements, and grown when a call needs more.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -68,9 +68,11 @@ __global__ void fwtc_plan_kernel(const int* __restrict__ dM, const int* __restri
                                  int mode, FwTcScratch s) {
   __shared__ int bin_tiles[kBins];
   __shared__ int bin_start[kBins];
+  __shared__ int kbin_jobs[kBins];  // pre-pass strips per quarter-octave of K
+  __shared__ int kbin_start[kBins];
   __shared__ unsigned long long ws_total;
   __shared__ int jobs_total;
-  for (int b = threadIdx.x; b < kBins; b += blockDim.x) bin_tiles[b] = 0;
+  for (int b = threadIdx.x; b < kBins; b += blockDim.x) bin_tiles[b] = kbin_jobs[b] = 0;
   if (threadIdx.x == 0) {
     ws_total = 0;
     jobs_total = 0;
@@ -106,12 +108,11 @@ __global__ void fwtc_plan_kernel(const int* __restrict__ dM, const int* __restri
     s.descs[i] = bad ? MatDesc{0, 0, 0, 1, 1, 1, pair_cfg(0), 0}
                      : MatDesc{M, N, K, max(M, 1), max(K, 1), max(M, 1),
                                best < 0 ? pair_cfg(0) : best, 0};
-    s.bins[i] = bin;
     s.mat_start[i] = best < 0 ? -1 : atomicAdd(&bin_tiles[bin], bt);
     // split-operand panels and pre-pass strips of a matrix with work
     PackDesc pd{};
     pd.kpad = bad ? 0 : (K * esz + 15) / 16 * 16 / esz;
-    int js = -1;
+    int js = -1, kbin = 0;
     if (best >= 0 && K > 0) {
       const unsigned long long a =
           ((unsigned long long)M * pd.kpad * esz + 255) & ~255ull;
@@ -122,10 +123,12 @@ __global__ void fwtc_plan_kernel(const int* __restrict__ dM, const int* __restri
       pd.a_lo = parts == 2 ? (long long)(off + a) : pd.a_hi;
       pd.b_hi = (long long)(off + parts * a);
       pd.b_lo = parts == 2 ? (long long)(off + parts * a + b) : pd.b_hi;
-      js = atomicAdd(&jobs_total, cdiv(M, 32) + cdiv(N, 32));
+      kbin = min(kBins - 1, (int)(4.0f * __log2f((float)K)));
+      js = atomicAdd(&kbin_jobs[kbin], cdiv(M, 32) + cdiv(N, 32));
     }
     s.pdescs[i] = pd;
     s.job_start[i] = js;
+    s.bins[i] = bin | (kbin << 8);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -133,6 +136,10 @@ __global__ void fwtc_plan_kernel(const int* __restrict__ dM, const int* __restri
     for (int b = kBins - 1; b >= 0; --b) {  // longest tiles first
       bin_start[b] = run;
       run += bin_tiles[b];
+    }
+    for (int b = kBins - 1; b >= 0; --b) {  // strips of the longest K first
+      kbin_start[b] = jobs_total;
+      jobs_total += kbin_jobs[b];
     }
     if (ws_total > s.cap_ws) {
       atomicOr(s.err, 2);
@@ -145,7 +152,9 @@ __global__ void fwtc_plan_kernel(const int* __restrict__ dM, const int* __restri
   __syncthreads();
   for (int i = threadIdx.x; i < batch; i += blockDim.x) {
     const int off = s.mat_start[i];
-    if (off >= 0) s.mat_start[i] = bin_start[s.bins[i]] + off;
+    if (off >= 0) s.mat_start[i] = bin_start[s.bins[i] & 0xff] + off;
+    const int js = s.job_start[i];
+    if (js >= 0) s.job_start[i] = kbin_start[s.bins[i] >> 8] + js;
   }
 }
 
@@ -205,12 +214,24 @@ bgemm_status_t fwtc_check_device(int dev) {
         return set_error(BGEMM_ERROR_INTERNAL, 0, -1, "no CTA-pair tile configuration is costed");
       if (err[0] & 2)
         return set_error(BGEMM_ERROR_NOT_SUPPORTED, 0, -1,
-                         "the batch's split operands exceed the workspace sized from max_dim "
-                         "and max_k; nothing was computed");
+                         "the batch's split operands exceed the workspace sized from "
+                         "max_operand_elems (or max_dim and max_k); nothing was computed");
       return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1,
                        "a matrix size was negative or above max_dim / max_k; such matrices were "
                        "skipped");
     }
+  }
+  return BGEMM_SUCCESS;
+}
+
+// Frees the tensor-core scratch of every mode on `dev`.
+bgemm_status_t fwtc_release(int dev) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto& kv : g_ctx) {
+    if (kv.first / 4 != dev || !kv.second.mem) continue;
+    const cudaError_t e = cudaFree(kv.second.mem);  // waits for kernels still using it
+    kv.second = FwTcContext{};
+    if (e != cudaSuccess) return cuda_error(e, "framework scratch release");
   }
   return BGEMM_SUCCESS;
 }
@@ -222,12 +243,12 @@ using namespace bgemm;
 extern "C" bgemm_status_t bgemm_framework_gemm_mode(const int* dM, const int* dN, const int* dK,
                                                     float* const* dA, float* const* dB,
                                                     float* const* dC, int batch, int max_dim,
-                                                    int max_k, bgemm_mode_t mode,
-                                                    bgemm_stream_t stream) {
+                                                    int max_k, long long max_operand_elems,
+                                                    bgemm_mode_t mode, bgemm_stream_t stream) {
   if (mode == BGEMM_MODE_SIMT_FP32)
     return bgemm_framework_gemm(dM, dN, dK, dA, dB, dC, nullptr, batch, max_dim, stream);
   if (mode < BGEMM_MODE_TF32 || mode > BGEMM_MODE_BF16X3)
-    return set_error(BGEMM_ERROR_INVALID_VALUE, 10, -1, "unknown mode %d", (int)mode);
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1, "unknown mode %d", (int)mode);
   if (batch < 0) return set_error(BGEMM_ERROR_INVALID_VALUE, 7, -1, "batch < 0");
   if (batch == 0) return BGEMM_SUCCESS;
   if (!dM) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "M is NULL");
@@ -240,6 +261,8 @@ extern "C" bgemm_status_t bgemm_framework_gemm_mode(const int* dM, const int* dN
     return set_error(BGEMM_ERROR_INVALID_VALUE, 8, -1, "max_dim = %d not in [1, 2^20]", max_dim);
   if (max_k < 1 || max_k > (1 << 24))
     return set_error(BGEMM_ERROR_INVALID_VALUE, 9, -1, "max_k = %d not in [1, 2^24]", max_k);
+  if (max_operand_elems < 0)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 10, -1, "max_operand_elems < 0");
   DeviceFacts df;
   bgemm_status_t st = device_facts(&df);
   if (st != BGEMM_SUCCESS) return st;
@@ -247,12 +270,16 @@ extern "C" bgemm_status_t bgemm_framework_gemm_mode(const int* dM, const int* dN
   const int kind = (mode == BGEMM_MODE_BF16X3) ? kKindBF16 : kKindTF32;
   const int split = (mode == BGEMM_MODE_TF32) ? 0 : 1;
   const size_t esz = kind == kKindBF16 ? 2 : 4;
-  const size_t kpad = ((size_t)max_k * esz + 15) / 16 * 16 / esz;
   const size_t tiles_per = (size_t)((max_dim + 255) / 256) * ((max_dim + 63) / 64);
   const size_t need_items = (size_t)batch * tiles_per;
   const size_t need_jobs = (size_t)batch * 2 * ((max_dim + 31) / 32);
+  // operand elements, plus each row's padding to 16 bytes and each panel's
+  // 256-byte alignment
+  const size_t elems = max_operand_elems > 0 ? (size_t)max_operand_elems
+                                             : (size_t)batch * 2 * max_dim * (size_t)max_k;
+  const size_t pad_elems = (size_t)batch * 2 * max_dim * (16 / esz - 1);
   const size_t need_ws =
-      (size_t)batch * (1 + split) * 2 * a256((size_t)max_dim * kpad * esz);
+      (size_t)(1 + split) * (esz * (elems + pad_elems) + (size_t)batch * 2 * 256);
 
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g_consts[df.device & 63]) {

@@ -124,5 +124,6 @@ int tc_debug_compare_tmaps(bgemm_plan_s* p, cudaStream_t stream, int* n_maps, in
 void tc_plan_release(bgemm_plan_s* p);
 // errors of the device-resident tensor-core path (framework_tc.cu)
 bgemm_status_t fwtc_check_device(int dev);
+bgemm_status_t fwtc_release(int dev);
 
 }  // namespace bgemm

@@ -55,6 +55,8 @@ constexpr int kThreads2 = 64 + kEpiWarps2 * 32;
 constexpr int kFineK2 = 64;
 // Matrices with K above kFineK2 promote every kGroupKB2 128-byte K slices.
 constexpr int kGroupKB2 = 2;
+// beta != 0: promotion groups before the tile's end at which C is prefetched
+constexpr int kCPrefetchLead = 2;
 
 __device__ __forceinline__ int snake(int c, int t, int ncl) {
   const int base = t * ncl;
@@ -295,7 +297,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       const int c_lo = half * kCols;
       const int ncols = max(0, min(kCols, bn - c_lo));
       const int col_base = ti.tn * bn + c_lo;
-      if (beta != 0.0f) c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
+
       const int nk = (d.K + KE - 1) / KE;
       const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
       const int ngroups = !SPLIT ? (nk > 0 ? 1 : 0)
@@ -304,7 +306,14 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
 #pragma unroll
       for (int j = 0; j < kCols; ++j) r[j] = 0.0f;
       int ok = 1;
+      // beta != 0: C is pulled into L2 kCPrefetchLead groups before the tile
+      // ends (earlier, the operand stream evicts it again before c_store)
+      const int g_pf = max(0, ngroups - kCPrefetchLead);
+      if (beta != 0.0f && ngroups == 0)
+        c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
       for (int g = 0; g < ngroups; ++g) {
+        if (beta != 0.0f && g == g_pf)
+          c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
         if (lane == 0) ok = wait_bounded(tfull(acc.idx), acc.phase, p.error, abort, p.timeout_ns);
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (!ok) break;
@@ -330,7 +339,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
         acc.next(kNAcc);
       }
       if (!ok) break;
-      c_store<kCols>(r, C, ldc, d.M, d.N, swap, row0, col_base, ncols, alpha, beta, lane);
+      c_store<kCols, 16>(r, C, ldc, d.M, d.N, swap, row0, col_base, ncols, alpha, beta, lane);
     }
   }
 

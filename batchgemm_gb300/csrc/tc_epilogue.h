@@ -9,9 +9,11 @@
 // transposed across the warp with shuffles, after which lanes again walk
 // consecutive m.
 //
-// With beta != 0 the old C is read.  c_prefetch pulls those lines into L2 when
-// the tile starts, so the final reads (issued in groups, all before the
-// stores of their group) hit L2 instead of waiting on HBM per element.
+// With beta != 0 the old C is read.  c_prefetch pulls those lines into L2
+// ahead of c_store (the one-SM kernel when a tile starts, the CTA-pair kernel
+// two promotion groups before a tile ends: earlier, the operand stream evicts
+// them again), so the final reads (issued in groups, all before the stores
+// of their group) hit L2 instead of waiting on HBM per element.
 #pragma once
 #include <stdint.h>
 
@@ -76,9 +78,9 @@ __device__ __forceinline__ void c_prefetch(const float* C, long long ldc, int M,
 // 0).  Swapped tiles transpose r in place.  Reads go kCRead at a time, all
 // before the stores of their elements (a store may alias a later load as far
 // as the compiler knows, so interleaving them would serialise every read).
-constexpr int kCRead = 8;  // C reads in flight per lane
+constexpr int kCRead = 8;  // C reads in flight per lane (default)
 
-template <int COLS>
+template <int COLS, int NRD = kCRead>
 __device__ __forceinline__ void c_store(float (&r)[COLS], float* C, long long ldc, int M, int N,
                                         bool swap, int row0, int col_base, int ncols, float alpha,
                                         float beta, int lane) {
@@ -106,13 +108,13 @@ __device__ __forceinline__ void c_store(float (&r)[COLS], float* C, long long ld
     step = ldc;
     float* base = C + m + (long long)n0 * ldc;
 #pragma unroll
-    for (int h = 0; h < 32; h += kCRead) {
-      float cv[kCRead];
+    for (int h = 0; h < 32; h += NRD) {
+      float cv[NRD];
 #pragma unroll
-      for (int j = 0; j < kCRead; ++j)
+      for (int j = 0; j < NRD; ++j)
         cv[j] = (rd && ok && h + j < nlim) ? base[(h + j) * step] : 0.0f;
 #pragma unroll
-      for (int j = 0; j < kCRead; ++j)
+      for (int j = 0; j < NRD; ++j)
         if (ok && h + j < nlim)
           base[(h + j) * step] =
               rd ? fmaf(alpha, r[c0 + h + j], beta * cv[j]) : alpha * r[c0 + h + j];

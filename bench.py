@@ -349,6 +349,39 @@ def gpu_leg(args, rank, world, local):
                 p2.close()
             except bg.BgemmError as e:
                 extra[mode] = {"unavailable": e.message}
+        # the same batch through the device-size entry (sizes and pointers in
+        # device arrays, tile queue / workspace / tensor maps built on the
+        # device; C += A B, so C is read as well), one captured call per step
+        dM, dN, dK = (torch.tensor(v, dtype=torch.int32, device=dev) for v in (w.M, w.N, w.K))
+        max_dim, max_k = max(max(w.M), max(w.N)), max(w.K)
+        elems = sum((m + n) * k for m, n, k in zip(w.M, w.N, w.K))
+        fw_args = (dM.data_ptr(), dN.data_ptr(), dK.data_ptr(), db.pA.data_ptr(),
+                   db.pB.data_ptr(), db.pC.data_ptr(), w.batch, max_dim, max_k, args.mode)
+        with torch.cuda.stream(s):
+            bg.framework_gemm_mode(*fw_args, stream=s, max_operand_elems=elems)
+        s.synchronize()
+        bg.framework_check_device(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            bg.framework_gemm_mode(*fw_args, stream=s, max_operand_elems=elems)
+        fw_steps = max(3, args.steps // 4)
+        with torch.cuda.stream(s):
+            for _ in range(3):
+                g.replay()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            for _ in range(fw_steps):
+                g.replay()
+            b.record(s)
+        s.synchronize()
+        bg.framework_check_device(s)
+        fw_ms = a.elapsed_time(b) / fw_steps
+        extra["device_sizes_" + args.mode] = {
+            "api": "bgemm_framework_gemm_mode (C += A B, sizes on the device)",
+            "tflops": round(flops / (fw_ms * 1e-3) / 1e12, 3), "ms_per_step": round(fw_ms, 4)}
+        del g
+        bg.framework_release()
     out["extra"] = extra
 
     # roofline of the dominant kernel: algorithmic flops of one launch over its

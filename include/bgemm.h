@@ -257,21 +257,31 @@ bgemm_status_t bgemm_framework_check_device(bgemm_stream_t stream);
  * table), the tile queue, the split-operand layout, the pre-pass strips and
  * the tensor maps are all built on the device, so the sizes never leave it
  * and a captured sequence of calls replays with whatever the size arrays
- * hold.  max_dim bounds every M_i and N_i, max_k every K_i: the library's
- * scratch (about batch * 2 * max_dim * max_k * 8 bytes of split operands for
- * TF32X3) is sized from them, and a matrix outside them is skipped and
- * reported by bgemm_framework_check_device, which also reports an expired
- * device wait (BGEMM_ERROR_DEVICE_TIMEOUT).  Calls in one mode on one device
- * share that scratch, so order them (one stream, or events between streams);
- * a call that grows it (the first, or larger batch / max_dim / max_k)
- * allocates and must not be inside a stream capture.  BGEMM_MODE_SIMT_FP32 is exactly
- * bgemm_framework_gemm (max_k unused).  Argument numbers: dM 1, dN 2, dK 3,
- * dA 4, dB 5, dC 6, batch 7, max_dim 8, max_k 9, mode 10. */
+ * hold.  max_dim bounds every M_i and N_i, max_k every K_i, and
+ * max_operand_elems the batch's sum of (M_i + N_i) * K_i (0: batch * 2 *
+ * max_dim * max_k); the library's scratch is sized from them (the split
+ * operands take 8 bytes per operand element for TF32X3, 4 for TF32 and
+ * BF16X3).  A matrix outside max_dim / max_k is skipped, a batch above
+ * max_operand_elems is not computed; bgemm_framework_check_device reports
+ * both, and an expired device wait (BGEMM_ERROR_DEVICE_TIMEOUT).  Calls in
+ * one mode on one device share that scratch, so order them (one stream, or
+ * events between streams); a call that grows it (the first, or larger
+ * bounds) allocates and must not be inside a stream capture.
+ * BGEMM_MODE_SIMT_FP32 is exactly bgemm_framework_gemm (max_k and
+ * max_operand_elems unused).  Argument numbers: dM 1, dN 2, dK 3, dA 4,
+ * dB 5, dC 6, batch 7, max_dim 8, max_k 9, max_operand_elems 10, mode 11. */
 bgemm_status_t bgemm_framework_gemm_mode(const int* dM, const int* dN,
                                          const int* dK, float* const* dA,
                                          float* const* dB, float* const* dC,
                                          int batch, int max_dim, int max_k,
+                                         long long max_operand_elems,
                                          bgemm_mode_t mode, bgemm_stream_t stream);
+
+/* Frees the scratch that bgemm_framework_gemm and bgemm_framework_gemm_mode
+ * keep on the current device (it is allocated again, at the size the next
+ * call needs).  Waits for the device; errors not yet collected by
+ * bgemm_framework_check_device are dropped.  No reference counterpart. */
+bgemm_status_t bgemm_framework_release(void);
 
 /* --- allocation-free variant of bgemm_framework_gemm ----------------------
  * No counterpart in the reference.  Same arguments and result as

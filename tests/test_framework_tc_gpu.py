@@ -146,6 +146,45 @@ def test_framework_mode_argument_errors(cuda):
         bg.framework_gemm_mode(*ptrs, 1, 16, 0, "tf32x3")
     assert (ei.value.status, ei.value.arg) == (1, 9)
     with pytest.raises(bg.BgemmError) as ei:
-        bg.framework_gemm_mode(*ptrs, 1, 16, 16, 7)
+        bg.framework_gemm_mode(*ptrs, 1, 16, 16, "tf32x3", max_operand_elems=-1)
     assert (ei.value.status, ei.value.arg) == (1, 10)
+    with pytest.raises(bg.BgemmError) as ei:
+        bg.framework_gemm_mode(*ptrs, 1, 16, 16, 7)
+    assert (ei.value.status, ei.value.arg) == (1, 11)
     bg.framework_gemm_mode(*ptrs, 0, 16, 16, "tf32x3")  # empty batch: nothing to do
+
+
+def test_framework_mode_operand_bound(cuda):
+    """max_operand_elems sizes the split-operand workspace from the batch's
+    actual sum of (M + N) * K instead of the batch * max_dim * max_k worst
+    case; a batch above the bound is not computed and is reported."""
+    M, N, K = shapes(77, 60, max_dim=600, max_k=800)
+    elems = sum((m + n) * k for m, n, k in zip(M, N, K))
+    db, host = make_batch(M, N, K, seed=31)
+    dM, dN, dK = dev(M), dev(N), dev(K)
+    call = lambda e: bg.framework_gemm_mode(dM.data_ptr(), dN.data_ptr(), dK.data_ptr(),
+                                            db.pA.data_ptr(), db.pB.data_ptr(),
+                                            db.pC.data_ptr(), len(M), 600, 800, "tf32x3",
+                                            max_operand_elems=e)
+    call(elems)
+    torch.cuda.synchronize()
+    bg.framework_check_device()
+    f64_check(db, host, db.C.cpu().numpy(), 1.0, 1.0, *FP64_BOUND["tf32x3"])
+    # scratch released, then sized for a tenth of the batch: nothing computed
+    bg.framework_release()
+    before = db.C.clone()
+    bg.framework_gemm_mode(dM.data_ptr(), dN.data_ptr(), dK.data_ptr(), db.pA.data_ptr(),
+                           db.pB.data_ptr(), db.pC.data_ptr(), len(M), 600, 800, "bf16x3",
+                           max_operand_elems=elems // 10)
+    torch.cuda.synchronize()
+    with pytest.raises(bg.BgemmError) as ei:
+        bg.framework_check_device()
+    assert ei.value.status == 2
+    assert torch.equal(db.C.isnan(), before.isnan())
+    assert torch.equal(torch.nan_to_num(db.C), torch.nan_to_num(before))
+    bg.framework_release()  # the next call sizes the scratch again
+    db.C.copy_(torch.from_numpy(host[2]))
+    call(elems)
+    torch.cuda.synchronize()
+    bg.framework_check_device()
+    f64_check(db, host, db.C.cpu().numpy(), 1.0, 1.0, *FP64_BOUND["tf32x3"])
