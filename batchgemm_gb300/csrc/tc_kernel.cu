@@ -187,8 +187,36 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const TcPackParams p) {
         }
         __syncthreads();
       }
+    } else if (((reinterpret_cast<uintptr_t>(X) | (uintptr_t)(ldx * 4)) & 15u) != 0) {
+      // rows of K that do not start on 16 bytes: a warp walks 4 rows, each
+      // load covering 32 consecutive k of one row (one coalesced run of 128
+      // bytes whatever the alignment; 8 threads per row with 4 scalar loads
+      // each would touch every sector of the run four times)
+      const int lane = tid & 31;
+      const int r_w = job.r0 + (tid >> 5) * 4;  // the warp's first row
+      for (int k0 = 0; k0 < K; k0 += kPackK) {
+        float x[4][kPackK / 32];
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+          const float* row = X + (long long)(r_w + rr) * ldx;
+#pragma unroll
+          for (int h = 0; h < kPackK / 32; ++h) {
+            const int k = k0 + 32 * h + lane;
+            x[rr][h] = (r_w + rr < rows && k < K) ? row[k] : 0.0f;
+          }
+        }
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+#pragma unroll
+          for (int h = 0; h < kPackK / 32; ++h) {
+            const int k = k0 + 32 * h + lane;
+            if (r_w + rr < rows && k < K)
+              put(hi, lo, (long long)(r_w + rr) * kpad + k, x[rr][h], p.kind, p.split);
+          }
+        }
+      }
     } else {
-      // already rows of K: 8 threads per row, four consecutive k each
+      // rows of K on 16 bytes: 8 threads per row, four consecutive k each
       const int nn = tid >> 3;
       const int n = job.r0 + nn;
       const int wk = (tid & 7) * 4;
