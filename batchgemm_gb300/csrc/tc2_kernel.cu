@@ -70,7 +70,10 @@ __device__ __forceinline__ uint32_t make_idesc_pair(int n) {
          ((uint32_t)(256 >> 4) << 24);
 }
 
-template <int KIND, int SPLIT>
+// BETA: the launch's beta is nonzero (C is read: late L2 prefetch, 16 reads in
+// flight).  The beta = 0 form is a separate instantiation that keeps the
+// plain epilogue's code (the read path's registers slowed it by ~4 %).
+template <int KIND, int SPLIT, bool BETA>
 __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmParams p) {
   using G = Geo2<SPLIT>;
   constexpr int kS = G::S;
@@ -297,7 +300,11 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       const int c_lo = half * kCols;
       const int ncols = max(0, min(kCols, bn - c_lo));
       const int col_base = ti.tn * bn + c_lo;
-
+      if constexpr (!BETA) {
+        // (never taken: this form is launched with beta = 0; the guarded
+        // tile-start prefetch keeps its code as measured fastest)
+        if (beta != 0.0f) c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
+      }
       const int nk = (d.K + KE - 1) / KE;
       const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
       const int ngroups = !SPLIT ? (nk > 0 ? 1 : 0)
@@ -308,11 +315,11 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       int ok = 1;
       // beta != 0: C is pulled into L2 kCPrefetchLead groups before the tile
       // ends (earlier, the operand stream evicts it again before c_store)
-      const int g_pf = max(0, ngroups - kCPrefetchLead);
-      if (beta != 0.0f && ngroups == 0)
+      const int g_pf = BETA ? max(0, ngroups - kCPrefetchLead) : -1;
+      if (BETA && ngroups == 0)
         c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
       for (int g = 0; g < ngroups; ++g) {
-        if (beta != 0.0f && g == g_pf)
+        if (BETA && g == g_pf)
           c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
         if (lane == 0) ok = wait_bounded(tfull(acc.idx), acc.phase, p.error, abort, p.timeout_ns);
         ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -339,7 +346,10 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
         acc.next(kNAcc);
       }
       if (!ok) break;
-      c_store<kCols, 16>(r, C, ldc, d.M, d.N, swap, row0, col_base, ncols, alpha, beta, lane);
+      if constexpr (BETA)
+        c_store<kCols, 16>(r, C, ldc, d.M, d.N, swap, row0, col_base, ncols, alpha, beta, lane);
+      else
+        c_store<kCols>(r, C, ldc, d.M, d.N, swap, row0, col_base, ncols, alpha, beta, lane);
     }
   }
 
@@ -350,11 +360,11 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
   if (warp == 1) tmem_dealloc_pair(tmem, 512);
 }
 
-template <int KIND, int SPLIT>
+template <int KIND, int SPLIT, bool BETA>
 cudaError_t launch2(const TcGemmParams& p, int grid, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc2_gemm_kernel<KIND, SPLIT>,
+    cudaError_t e = cudaFuncSetAttribute(tc2_gemm_kernel<KIND, SPLIT, BETA>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          Geo2<SPLIT>::SMEM);
     if (e != cudaSuccess) return e;
@@ -372,7 +382,13 @@ cudaError_t launch2(const TcGemmParams& p, int grid, cudaStream_t s) {
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, tc2_gemm_kernel<KIND, SPLIT>, p);
+  return cudaLaunchKernelEx(&cfg, tc2_gemm_kernel<KIND, SPLIT, BETA>, p);
+}
+
+template <int KIND, int SPLIT>
+cudaError_t launch2b(const TcGemmParams& p, int grid, cudaStream_t s) {
+  return p.beta != 0.0f ? launch2<KIND, SPLIT, true>(p, grid, s)
+                        : launch2<KIND, SPLIT, false>(p, grid, s);
 }
 
 }  // namespace
@@ -380,9 +396,9 @@ cudaError_t launch2(const TcGemmParams& p, int grid, cudaStream_t s) {
 cudaError_t tc2_gemm_launch(int kind, int split, const TcGemmParams& p, int grid,
                             cudaStream_t s) {
   if (grid < 2 || (grid & 1)) return cudaErrorInvalidValue;
-  if (kind == kKindTF32 && !split) return launch2<kKindTF32, 0>(p, grid, s);
-  if (kind == kKindTF32) return launch2<kKindTF32, 1>(p, grid, s);
-  if (kind == kKindBF16 && split) return launch2<kKindBF16, 1>(p, grid, s);
+  if (kind == kKindTF32 && !split) return launch2b<kKindTF32, 0>(p, grid, s);
+  if (kind == kKindTF32) return launch2b<kKindTF32, 1>(p, grid, s);
+  if (kind == kKindBF16 && split) return launch2b<kKindBF16, 1>(p, grid, s);
   return cudaErrorInvalidValue;
 }
 
@@ -399,9 +415,9 @@ int tc2_max_clusters() {
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaFuncSetAttribute(tc2_gemm_kernel<kKindTF32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(tc2_gemm_kernel<kKindTF32, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        kSmemMax);
-  if (cudaOccupancyMaxActiveClusters(&n, tc2_gemm_kernel<kKindTF32, 1>, &cfg) != cudaSuccess)
+  if (cudaOccupancyMaxActiveClusters(&n, tc2_gemm_kernel<kKindTF32, 1, true>, &cfg) != cudaSuccess)
     return 0;
   return n;
 }
