@@ -86,6 +86,25 @@ def test_no_cpu_fallback_without_gpu(built_lib):
     assert ei.value.status in (2, 4)
 
 
+def test_framework_mode_argument_checks_without_gpu(built_lib):
+    """The device-size entry checks its arguments before touching a device:
+    BLAS-style numbers (dM 1 .. max_operand_elems 10, mode 11); an empty
+    batch is a no-op."""
+    p = 8  # any non-null address: never dereferenced by the checks
+    args = lambda **kw: [kw.get(k, d) for k, d in (
+        ("dM", p), ("dN", p), ("dK", p), ("dA", p), ("dB", p), ("dC", p), ("batch", 1),
+        ("max_dim", 16), ("max_k", 16), ("mode", "tf32x3"))]
+    for kw, argpos in ((dict(mode=9), 11), (dict(batch=-1), 7), (dict(dK=None), 3),
+                       (dict(dC=None), 6), (dict(max_dim=0), 8), (dict(max_k=0), 9)):
+        with pytest.raises(bg.BgemmError) as ei:
+            bg.framework_gemm_mode(*args(**kw))
+        assert (ei.value.status, ei.value.arg) == (1, argpos), kw
+    with pytest.raises(bg.BgemmError) as ei:
+        bg.framework_gemm_mode(*args(), max_operand_elems=-5)
+    assert ei.value.arg == 10
+    bg.framework_gemm_mode(*args(batch=0))
+
+
 def simt_queue(M, N, K, slots=304, force=-1, rebalance=True):
     L = bg.lib()
     n = len(M)
