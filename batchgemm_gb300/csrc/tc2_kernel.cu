@@ -58,6 +58,15 @@ constexpr int kGroupKB2 = 2;
 // beta != 0: promotion groups before the tile's end at which C is prefetched
 constexpr int kCPrefetchLead = 2;
 
+// MMA width of a tile along the B side: bn, or for the matrix's last tile
+// column its remaining width rounded up to 16 (the pair MMA's N step), so
+// that the padding of a ragged edge is not multiplied.  CTA r then loads
+// B-side rows [tn*bn + r*n/2, +n/2), the columns stay contiguous.
+__device__ __forceinline__ int tile_n(const MatDesc& d, int tn, int bn) {
+  const int rem = (tc_cfg_swap(d.cfg) ? d.M : d.N) - tn * bn;
+  return min(bn, (rem + 15) & ~15);
+}
+
 __device__ __forceinline__ int snake(int c, int t, int ncl) {
   const int base = t * ncl;
   return (t & 1) ? base + (ncl - 1 - c) : base + c;
@@ -152,7 +161,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
         const int nk = (d.K + KE - 1) / KE;
         const uint32_t tx = 2u * G::NP * (uint32_t)(kA + hb * 128);  // both CTAs, all parts
         const int row_a = ti.tm * 256 + (int)rank * kRows;
-        const int row_b = ti.tn * bn + (int)rank * hb;
+        const int row_b = ti.tn * bn + (int)rank * (tile_n(d, ti.tn, bn) >> 1);
         for (int kb = 0; kb < nk; ++kb) {
           if (!wait_bounded(empty(st.idx), st.phase ^ 1u, p.error, abort, p.timeout_ns)) {
             ok = false;
@@ -200,7 +209,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
         const TileItem ti = p.items[it];
         const MatDesc d = p.descs[ti.mat];
         const int bn = tc2_cfg_bn(d.cfg);
-        const uint32_t idesc = make_idesc_pair<KIND>(bn);
+        const uint32_t idesc = make_idesc_pair<KIND>(tile_n(d, ti.tn, bn));
         const int nk = (d.K + KE - 1) / KE;
         const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
         const bool fine = SPLIT && d.K <= kFineK2;
@@ -298,7 +307,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       const int row0 = ti.tm * 256 + (int)rank * kRows + q * 32;  // A-side row of lane 0
       const long long ldc = d.ldc;
       const int c_lo = half * kCols;
-      const int ncols = max(0, min(kCols, bn - c_lo));
+      const int ncols = max(0, min(kCols, tile_n(d, ti.tn, bn) - c_lo));
       const int col_base = ti.tn * bn + c_lo;
       if constexpr (!BETA) {
         // (never taken: this form is launched with beta = 0; the guarded
