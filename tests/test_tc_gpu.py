@@ -155,6 +155,8 @@ def test_every_tile_config(cuda, cfg):
     K = rng.integers(1, 200, 10).tolist()
     for mode in ("tf32x3", "bf16x3"):
         run_mode(mode, M, N, K, 1.0, 0.25, force=cfg, seed=cfg)
+    # beta = 0 runs the pair kernel's separate beta-free instantiation
+    run_mode("tf32x3", M, N, K, 1.0, 0.0, force=cfg, seed=cfg + 1)
     run_mode("tf32", M, N, K, 0.5, 0.0, force=cfg, seed=cfg)
 
 
