@@ -273,6 +273,9 @@ extern "C" bgemm_status_t bgemm_framework_gemm_mode(const int* dM, const int* dN
   const size_t tiles_per = (size_t)((max_dim + 255) / 256) * ((max_dim + 63) / 64);
   const size_t need_items = (size_t)batch * tiles_per;
   const size_t need_jobs = (size_t)batch * 2 * ((max_dim + 31) / 32);
+  if (need_items > (size_t)INT32_MAX || need_jobs > (size_t)INT32_MAX)
+    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 8, -1,
+                     "batch %d with max_dim %d can hold more than 2^31 tiles", batch, max_dim);
   // operand elements, plus each row's padding to 16 bytes and each panel's
   // 256-byte alignment
   const size_t elems = max_operand_elems > 0 ? (size_t)max_operand_elems
