@@ -22,6 +22,7 @@
 #include <cstring>
 #include <mutex>
 #include <unordered_map>
+#include <vector>
 
 #include "bgemm.h"
 #include "plan_internal.h"
@@ -61,7 +62,63 @@ struct FwTcScratch {
   unsigned long long cap_ws;
 };
 
-__device__ __forceinline__ int cdiv(int a, int b) { return (a + b - 1) / b; }
+__host__ __device__ __forceinline__ int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+// What the planner decides for one matrix, independently of the others; the
+// kernel then reserves queue slots, strips and workspace with atomics, and a
+// host replay (bgemm_debug_framework_tc_plan) with plain sums.
+struct FwTcMat {
+  MatDesc desc;
+  int kpad;        // packed row length (elements)
+  int bad;         // size negative or above max_dim / max_k: skipped
+  int nocfg;       // no costed CTA-pair configuration: skipped
+  int tiles;       // work items (0: none)
+  int bin;         // quarter-octave bin of the modelled tile time
+  int kbin;        // quarter-octave bin of K (strips of the longest K first)
+  int strips;      // pre-pass strips (0: nothing to pack)
+  unsigned long long a_bytes, b_bytes;  // one part of each operand, 256-byte aligned
+};
+
+__host__ __device__ inline FwTcMat fwtc_plan_matrix(int M, int N, int K, int max_dim, int max_k,
+                                                    int mode, const TileCost* cost) {
+  FwTcMat r{};
+  const int esz = (mode == BGEMM_MODE_BF16X3) ? 2 : 4;
+  r.bad = M < 0 || N < 0 || K < 0 || M > max_dim || N > max_dim || K > max_k;
+  int best = -1;
+  if (!r.bad && M > 0 && N > 0) {
+    float bw = 0.f, btt = 0.f;
+    int bt = 0;
+    for (int q = 5; q >= 0; --q) {
+      const int c = pair_cfg(q);
+      const TileCost tc = cost[c];
+      if (tc.b_ns <= 0.f) continue;
+      const bool swap = tc_cfg_swap(c);
+      const int ra = swap ? N : M, rb = swap ? M : N;
+      const int t = cdiv(ra, 256) * cdiv(rb, tc2_cfg_bn(c));
+      const float tt = tc.a_ns + tc.b_ns * (float)K;
+      const float w = (float)t * tt;
+      if (best < 0 || w < bw * 0.999f) { best = c; bt = t; bw = w; btt = tt; }
+    }
+    if (best >= 0) {
+      r.tiles = bt;
+      r.bin = min(kBins - 1, max(0, (int)(4.0f * log2f(fmaxf(btt, 1.0f)) - 24.0f)));
+    } else {
+      r.nocfg = 1;
+    }
+  }
+  // a skipped matrix keeps an empty descriptor (no maps, strips or tiles)
+  r.desc = r.bad ? MatDesc{0, 0, 0, 1, 1, 1, pair_cfg(0), 0}
+                 : MatDesc{M, N, K, max(M, 1), max(K, 1), max(M, 1),
+                           best < 0 ? pair_cfg(0) : best, 0};
+  r.kpad = r.bad ? 0 : (K * esz + 15) / 16 * 16 / esz;
+  if (best >= 0 && K > 0) {
+    r.a_bytes = ((unsigned long long)M * r.kpad * esz + 255) & ~255ull;
+    r.b_bytes = ((unsigned long long)N * r.kpad * esz + 255) & ~255ull;
+    r.kbin = min(kBins - 1, (int)(4.0f * log2f((float)K)));
+    r.strips = cdiv(M, 32) + cdiv(N, 32);
+  }
+  return r;
+}
 
 __global__ void fwtc_plan_kernel(const int* __restrict__ dM, const int* __restrict__ dN,
                                  const int* __restrict__ dK, int batch, int max_dim, int max_k,
@@ -78,57 +135,29 @@ __global__ void fwtc_plan_kernel(const int* __restrict__ dM, const int* __restri
     jobs_total = 0;
   }
   __syncthreads();
-  const int esz = (mode == BGEMM_MODE_BF16X3) ? 2 : 4;
   const int parts = (mode == BGEMM_MODE_TF32) ? 1 : 2;
   for (int i = threadIdx.x; i < batch; i += blockDim.x) {
-    const int M = dM[i], N = dN[i], K = dK[i];
-    const bool bad = M < 0 || N < 0 || K < 0 || M > max_dim || N > max_dim || K > max_k;
-    if (bad) atomicOr(s.err, 1);
-    int best = -1, bin = 0;
-    int bt = 0;
-    if (!bad && M > 0 && N > 0) {
-      float bw = 0.f, btt = 0.f;
-      for (int q = 5; q >= 0; --q) {
-        const int c = pair_cfg(q);
-        const TileCost tc = c_tc_cost[mode - 1][c];
-        if (tc.b_ns <= 0.f) continue;
-        const bool swap = tc_cfg_swap(c);
-        const int ra = swap ? N : M, rb = swap ? M : N;
-        const int t = cdiv(ra, 256) * cdiv(rb, tc2_cfg_bn(c));
-        const float tt = tc.a_ns + tc.b_ns * (float)K;
-        const float w = (float)t * tt;
-        if (best < 0 || w < bw * 0.999f) { best = c; bt = t; bw = w; btt = tt; }
-      }
-      if (best >= 0)
-        bin = min(kBins - 1, max(0, (int)(4.0f * __log2f(fmaxf(btt, 1.0f)) - 24.0f)));
-      else
-        atomicOr(s.err, 4);  // no CTA-pair configuration in the cost table
-    }
-    // a skipped matrix keeps an empty descriptor (no maps, strips or tiles)
-    s.descs[i] = bad ? MatDesc{0, 0, 0, 1, 1, 1, pair_cfg(0), 0}
-                     : MatDesc{M, N, K, max(M, 1), max(K, 1), max(M, 1),
-                               best < 0 ? pair_cfg(0) : best, 0};
-    s.mat_start[i] = best < 0 ? -1 : atomicAdd(&bin_tiles[bin], bt);
+    const FwTcMat r = fwtc_plan_matrix(dM[i], dN[i], dK[i], max_dim, max_k, mode,
+                                       c_tc_cost[mode - 1]);
+    if (r.bad) atomicOr(s.err, 1);
+    if (r.nocfg) atomicOr(s.err, 4);
+    s.descs[i] = r.desc;
+    s.mat_start[i] = r.tiles ? atomicAdd(&bin_tiles[r.bin], r.tiles) : -1;
     // split-operand panels and pre-pass strips of a matrix with work
     PackDesc pd{};
-    pd.kpad = bad ? 0 : (K * esz + 15) / 16 * 16 / esz;
-    int js = -1, kbin = 0;
-    if (best >= 0 && K > 0) {
-      const unsigned long long a =
-          ((unsigned long long)M * pd.kpad * esz + 255) & ~255ull;
-      const unsigned long long b =
-          ((unsigned long long)N * pd.kpad * esz + 255) & ~255ull;
-      const unsigned long long off = atomicAdd(&ws_total, parts * (a + b));
+    pd.kpad = r.kpad;
+    int js = -1;
+    if (r.strips) {
+      const unsigned long long off = atomicAdd(&ws_total, parts * (r.a_bytes + r.b_bytes));
       pd.a_hi = (long long)off;
-      pd.a_lo = parts == 2 ? (long long)(off + a) : pd.a_hi;
-      pd.b_hi = (long long)(off + parts * a);
-      pd.b_lo = parts == 2 ? (long long)(off + parts * a + b) : pd.b_hi;
-      kbin = min(kBins - 1, (int)(4.0f * __log2f((float)K)));
-      js = atomicAdd(&kbin_jobs[kbin], cdiv(M, 32) + cdiv(N, 32));
+      pd.a_lo = parts == 2 ? (long long)(off + r.a_bytes) : pd.a_hi;
+      pd.b_hi = (long long)(off + parts * r.a_bytes);
+      pd.b_lo = parts == 2 ? (long long)(off + parts * r.a_bytes + r.b_bytes) : pd.b_hi;
+      js = atomicAdd(&kbin_jobs[r.kbin], r.strips);
     }
     s.pdescs[i] = pd;
     s.job_start[i] = js;
-    s.bins[i] = bin | (kbin << 8);
+    s.bins[i] = r.bin | (r.kbin << 8);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -190,6 +219,33 @@ std::unordered_map<long long, FwTcContext> g_ctx;  // key: device * 4 + mode
 bool g_consts[64] = {};
 
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// The cost table with the host planner's rule for untuned entries: the
+// 3xTF32 cost of the same tile, halved per unit of K for one-part modes.
+void fwtc_cost_table(TileCost (&cost)[3][16]) {
+  for (int m = 0; m < 3; ++m)
+    for (int c = 0; c < 16; ++c) {
+      cost[m][c] = kTcCost[m][c];
+      const TileCost& t3 = kTcCost[BGEMM_MODE_TF32X3 - 1][c];
+      if (cost[m][c].b_ns <= 0.0f && t3.b_ns > 0.0f)
+        cost[m][c] = TileCost{t3.a_ns, m == BGEMM_MODE_TF32X3 - 1 ? t3.b_ns : 0.5f * t3.b_ns};
+    }
+}
+
+// Scratch a call needs: queue items, pre-pass strips, split-operand bytes.
+void fwtc_capacity(int batch, int max_dim, int max_k, long long max_operand_elems, int mode,
+                   size_t* items, size_t* jobs, size_t* ws) {
+  const size_t esz = (mode == BGEMM_MODE_BF16X3) ? 2 : 4;
+  const size_t parts = (mode == BGEMM_MODE_TF32) ? 1 : 2;
+  *items = (size_t)batch * ((max_dim + 255) / 256) * ((max_dim + 63) / 64);
+  *jobs = (size_t)batch * 2 * ((max_dim + 31) / 32);
+  // operand elements, plus each row's padding to 16 bytes and each panel's
+  // 256-byte alignment
+  const size_t elems = max_operand_elems > 0 ? (size_t)max_operand_elems
+                                             : (size_t)batch * 2 * max_dim * (size_t)max_k;
+  const size_t pad_elems = (size_t)batch * 2 * max_dim * (16 / esz - 1);
+  *ws = parts * (esz * (elems + pad_elems) + (size_t)batch * 2 * 256);
+}
 
 }  // namespace
 
@@ -263,39 +319,22 @@ extern "C" bgemm_status_t bgemm_framework_gemm_mode(const int* dM, const int* dN
     return set_error(BGEMM_ERROR_INVALID_VALUE, 9, -1, "max_k = %d not in [1, 2^24]", max_k);
   if (max_operand_elems < 0)
     return set_error(BGEMM_ERROR_INVALID_VALUE, 10, -1, "max_operand_elems < 0");
+  size_t need_items, need_jobs, need_ws;
+  fwtc_capacity(batch, max_dim, max_k, max_operand_elems, mode, &need_items, &need_jobs, &need_ws);
+  if (need_items > (size_t)INT32_MAX || need_jobs > (size_t)INT32_MAX)
+    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 8, -1,
+                     "batch %d with max_dim %d can hold more than 2^31 tiles", batch, max_dim);
   DeviceFacts df;
   bgemm_status_t st = device_facts(&df);
   if (st != BGEMM_SUCCESS) return st;
 
   const int kind = (mode == BGEMM_MODE_BF16X3) ? kKindBF16 : kKindTF32;
   const int split = (mode == BGEMM_MODE_TF32) ? 0 : 1;
-  const size_t esz = kind == kKindBF16 ? 2 : 4;
-  const size_t tiles_per = (size_t)((max_dim + 255) / 256) * ((max_dim + 63) / 64);
-  const size_t need_items = (size_t)batch * tiles_per;
-  const size_t need_jobs = (size_t)batch * 2 * ((max_dim + 31) / 32);
-  if (need_items > (size_t)INT32_MAX || need_jobs > (size_t)INT32_MAX)
-    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 8, -1,
-                     "batch %d with max_dim %d can hold more than 2^31 tiles", batch, max_dim);
-  // operand elements, plus each row's padding to 16 bytes and each panel's
-  // 256-byte alignment
-  const size_t elems = max_operand_elems > 0 ? (size_t)max_operand_elems
-                                             : (size_t)batch * 2 * max_dim * (size_t)max_k;
-  const size_t pad_elems = (size_t)batch * 2 * max_dim * (16 / esz - 1);
-  const size_t need_ws =
-      (size_t)(1 + split) * (esz * (elems + pad_elems) + (size_t)batch * 2 * 256);
 
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g_consts[df.device & 63]) {
-    // the cost table with the host planner's rule for untuned entries: the
-    // 3xTF32 cost of the same tile, halved per unit of K for one-part modes
     TileCost cost[3][16];
-    for (int m = 0; m < 3; ++m)
-      for (int c = 0; c < 16; ++c) {
-        cost[m][c] = kTcCost[m][c];
-        const TileCost& t3 = kTcCost[BGEMM_MODE_TF32X3 - 1][c];
-        if (cost[m][c].b_ns <= 0.0f && t3.b_ns > 0.0f)
-          cost[m][c] = TileCost{t3.a_ns, m == BGEMM_MODE_TF32X3 - 1 ? t3.b_ns : 0.5f * t3.b_ns};
-      }
+    fwtc_cost_table(cost);
     cudaError_t e = cudaMemcpyToSymbol(c_tc_cost, cost, sizeof(cost));
     if (e != cudaSuccess) return cuda_error(e, "framework constants");
     g_consts[df.device & 63] = true;
@@ -381,4 +420,89 @@ extern "C" bgemm_status_t bgemm_framework_gemm_mode(const int* dM, const int* dN
   e = tc2_gemm_launch(kind, split, gp, 2 * clusters, stream);
   if (e != cudaSuccess) return cuda_error(e, "tcgen05 GEMM launch");
   return BGEMM_SUCCESS;
+}
+
+// Host replay of the device planner (fwtc_plan_kernel + fwtc_expand_kernel)
+// for tests without a GPU: the same per-matrix decisions, the reservations
+// made in matrix order instead of by atomics.
+extern "C" int bgemm_debug_framework_tc_plan(const int* M, const int* N, const int* K, int batch,
+                                             int max_dim, int max_k, long long max_operand_elems,
+                                             int mode, int* items_out, int max_items,
+                                             int* jobs_out, int max_jobs, long long* ws_out,
+                                             int* n_jobs, long long* ws_used,
+                                             long long* ws_capacity, int* err) {
+  if (batch < 0 || mode < BGEMM_MODE_TF32 || mode > BGEMM_MODE_BF16X3 || !n_jobs || !ws_used ||
+      !ws_capacity || !err || (batch > 0 && (!M || !N || !K)))
+    return -1;
+  TileCost cost[3][16];
+  fwtc_cost_table(cost);
+  size_t cap_items, cap_jobs, cap_ws;
+  fwtc_capacity(batch, max_dim, max_k, max_operand_elems, mode, &cap_items, &cap_jobs, &cap_ws);
+  const unsigned long long parts = (mode == BGEMM_MODE_TF32) ? 1 : 2;
+  std::vector<FwTcMat> r(batch);
+  std::vector<int> mat_start(batch, -1), job_start(batch, -1);
+  int bin_tiles[kBins] = {}, kbin_jobs[kBins] = {};
+  unsigned long long ws_total = 0;
+  *err = 0;
+  for (int i = 0; i < batch; ++i) {
+    r[i] = fwtc_plan_matrix(M[i], N[i], K[i], max_dim, max_k, mode, cost[mode - 1]);
+    if (r[i].bad) *err |= 1;
+    if (r[i].nocfg) *err |= 4;
+    if (r[i].tiles) {
+      mat_start[i] = bin_tiles[r[i].bin];
+      bin_tiles[r[i].bin] += r[i].tiles;
+    }
+    long long off[4] = {0, 0, 0, 0};
+    if (r[i].strips) {
+      const unsigned long long o = ws_total;
+      ws_total += parts * (r[i].a_bytes + r[i].b_bytes);
+      off[0] = (long long)o;
+      off[1] = parts == 2 ? (long long)(o + r[i].a_bytes) : off[0];
+      off[2] = (long long)(o + parts * r[i].a_bytes);
+      off[3] = parts == 2 ? (long long)(o + parts * r[i].a_bytes + r[i].b_bytes) : off[2];
+      job_start[i] = kbin_jobs[r[i].kbin];
+      kbin_jobs[r[i].kbin] += r[i].strips;
+    }
+    if (ws_out) {
+      for (int q = 0; q < 4; ++q) ws_out[5 * i + q] = off[q];
+      ws_out[5 * i + 4] = r[i].kpad;
+    }
+  }
+  int bin_start[kBins], kbin_start[kBins], n_items = 0, nj = 0;
+  for (int b = kBins - 1; b >= 0; --b) {
+    bin_start[b] = n_items;
+    n_items += bin_tiles[b];
+    kbin_start[b] = nj;
+    nj += kbin_jobs[b];
+  }
+  *ws_used = (long long)ws_total;
+  *ws_capacity = (long long)cap_ws;
+  if (ws_total > cap_ws) {
+    *err |= 2;
+    n_items = 0;
+    nj = 0;
+  }
+  *n_jobs = nj;
+  if ((items_out && n_items > max_items) || (jobs_out && nj > max_jobs)) return -1;
+  for (int i = 0; i < batch && n_items > 0; ++i) {
+    if (mat_start[i] < 0) continue;
+    const MatDesc& d = r[i].desc;
+    const bool swap = tc_cfg_swap(d.cfg);
+    const int tmx = cdiv(swap ? d.N : d.M, 256), tnx = cdiv(swap ? d.M : d.N, tc2_cfg_bn(d.cfg));
+    const int start = bin_start[r[i].bin] + mat_start[i];
+    for (int t = 0; items_out && t < tmx * tnx; ++t) {
+      items_out[3 * (start + t)] = i;
+      items_out[3 * (start + t) + 1] = t % tmx;
+      items_out[3 * (start + t) + 2] = t / tmx;
+    }
+    if (job_start[i] < 0) continue;
+    const int js = kbin_start[r[i].kbin] + job_start[i];
+    const int sa = cdiv(d.M, 32), sb = cdiv(d.N, 32);
+    for (int j = 0; jobs_out && j < sa + sb; ++j) {
+      jobs_out[3 * (js + j)] = i;
+      jobs_out[3 * (js + j) + 1] = j < sa ? 0 : 1;
+      jobs_out[3 * (js + j) + 2] = 32 * (j < sa ? j : j - sa);
+    }
+  }
+  return n_items;
 }

@@ -42,6 +42,22 @@ int bgemm_debug_tc_plan(const int* M, const int* N, const int* K, int batch, int
                         int max_items, long long* ws_out, int* jobs_out, int max_jobs,
                         int* n_jobs, long long* ws_bytes, int* kernel_family);
 
+/* Host replay of the planner that bgemm_framework_gemm_mode runs on the
+ * device (same per-matrix tile choice, bins and reservations, made in matrix
+ * order instead of by atomics).  items_out[3*max_items]: (matrix, tile along
+ * the MMA's M side, tile along its N side) in queue order; jobs_out
+ * [3*max_jobs]: pre-pass strips (matrix, operand, first row); ws_out[5*batch]:
+ * A hi, A lo, B hi, B lo byte offsets and kpad.  *n_jobs, *ws_used (bytes of
+ * split operands), *ws_capacity (the scratch the entry sizes from its bounds)
+ * and *err (the device error bits: 1 size out of bounds, 2 workspace too
+ * small, 4 no costed configuration) are always written.  Returns the number
+ * of work items, or -1 on invalid arguments or too small output arrays. */
+int bgemm_debug_framework_tc_plan(const int* M, const int* N, const int* K, int batch,
+                                  int max_dim, int max_k, long long max_operand_elems, int mode,
+                                  int* items_out, int max_items, int* jobs_out, int max_jobs,
+                                  long long* ws_out, int* n_jobs, long long* ws_used,
+                                  long long* ws_capacity, int* err);
+
 /* Tensor-core plans: waits for `stream`, encodes on the host the tensor maps
  * that the device built for the plan, and compares them byte by byte.
  * *n_maps receives the number of maps compared, *n_diff how many differ,

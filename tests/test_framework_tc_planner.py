@@ -1,0 +1,154 @@
+"""Host replay of the device-side planner of bgemm_framework_gemm_mode
+(bgemm_debug_framework_tc_plan), without a GPU.
+
+The same per-matrix decisions as fwtc_plan_kernel (tile configuration from the
+cost table, bins, strips, workspace panels), reserved in matrix order instead
+of by atomics.  For random batches with empty, K = 0, one-row and
+out-of-bounds matrices, in every tensor-core mode:
+  * every output tile of every in-bounds matrix is in the queue exactly once,
+    a matrix's tiles adjacent;
+  * every 32-row strip of A and B of a matrix with work is a pre-pass job
+    exactly once, grouped by matrix, the longest K (quarter-octave bins) first;
+  * the split-operand panels are 256-byte aligned, disjoint, and fit the
+    scratch the entry sizes from max_dim / max_k or from the operand bound;
+  * out-of-bounds sizes and a too small operand bound raise the error bits
+    the device reports.
+"""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+import batchgemm_gb300 as bg
+
+MODES = {"tf32": 1, "tf32x3": 2, "bf16x3": 3}
+
+
+def fw_plan(M, N, K, max_dim, max_k, mode, elems=0):
+    L = bg.lib()
+    n = len(M)
+    ia = lambda v: (ctypes.c_int * max(n, 1))(*v)
+    nj, used, cap, err = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
+    f = L.bgemm_debug_framework_tc_plan
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 3 + [ctypes.c_longlong, ctypes.c_int,
+                                                              ctypes.c_void_p, ctypes.c_int,
+                                                              ctypes.c_void_p, ctypes.c_int] + \
+        [ctypes.c_void_p] * 5
+    args = lambda items, mi, jobs, mj, ws: (ia(M), ia(N), ia(K), n, max_dim, max_k, elems,
+                                            MODES[mode], items, mi, jobs, mj, ws,
+                                            ctypes.byref(nj), ctypes.byref(used),
+                                            ctypes.byref(cap), ctypes.byref(err))
+    cnt = f(*args(None, 0, None, 0, None))
+    assert cnt >= 0
+    items = (ctypes.c_int * max(3 * cnt, 1))()
+    jobs = (ctypes.c_int * max(3 * nj.value, 1))()
+    ws = (ctypes.c_longlong * max(5 * n, 1))()
+    cnt2 = f(*args(items, cnt, jobs, nj.value, ws))
+    assert cnt2 == cnt
+    return (np.array(items[:3 * cnt]).reshape(-1, 3), np.array(jobs[:3 * nj.value]).reshape(-1, 3),
+            np.array(ws[:5 * n]).reshape(-1, 5), used.value, cap.value, err.value)
+
+
+def batch(seed, n=80, max_dim=900, max_k=700):
+    rng = np.random.default_rng(seed)
+    M = np.exp(rng.uniform(0, np.log(max_dim), n)).astype(int).tolist()
+    N = np.exp(rng.uniform(0, np.log(max_dim), n)).astype(int).tolist()
+    K = np.exp(rng.uniform(0, np.log(max_k), n)).astype(int).tolist()
+    M[:6] = [0, 5, 1, max_dim, 2, 700]
+    N[:6] = [9, 0, max_dim, 1, 3, 600]
+    K[:6] = [4, 4, 17, max_k, 0, 300]
+    return M, N, K
+
+
+def check_plan(M, N, K, mode, items, jobs, ws, used, cap, in_bounds):
+    # tiles: each exactly once, a matrix's tiles adjacent
+    seen = set()
+    order = []
+    for mat, tm, tn in items:
+        key = (mat, tm, tn)
+        assert key not in seen
+        seen.add(key)
+        if not order or order[-1] != mat:
+            assert mat not in order, "tiles of matrix %d are not adjacent" % mat
+            order.append(mat)
+    for i in range(len(M)):
+        got = {k for k in seen if k[0] == i}
+        if not (in_bounds[i] and M[i] and N[i]):
+            assert not got
+            continue
+        # the tile grid is 256 rows on one side and 64/128/256 on the other
+        sides = sorted((1 + max(k[1] for k in got), 1 + max(k[2] for k in got)))
+        ok = False
+        for bn in (64, 128, 256):
+            for ra, rb in ((M[i], N[i]), (N[i], M[i])):
+                if [-(-ra // 256), -(-rb // bn)] in ([sides[0], sides[1]], [sides[1], sides[0]]):
+                    ok = True
+        assert ok, "matrix %d (%dx%d): tile grid %s" % (i, M[i], N[i], sides)
+        assert len(got) == sides[0] * sides[1]
+    # strips: every 32-row strip once, grouped by matrix, longest K first
+    strips = [tuple(j) for j in jobs]
+    assert len(set(strips)) == len(strips)
+    work = [i for i in range(len(M)) if in_bounds[i] and M[i] and N[i] and K[i]]
+    want = {(i, 0, r) for i in work for r in range(0, M[i], 32)}
+    want |= {(i, 1, r) for i in work for r in range(0, N[i], 32)}
+    assert set(strips) == want
+    mats = []
+    for mat, _, _ in strips:
+        if not mats or mats[-1] != mat:
+            assert mat not in mats
+            mats.append(mat)
+    kbins = [min(63, int(4 * math.log2(K[m]))) for m in mats]
+    assert kbins == sorted(kbins, reverse=True)
+    # workspace panels: aligned, disjoint, inside the scratch
+    esz = 2 if mode == "bf16x3" else 4
+    split = mode != "tf32"
+    spans = []
+    for i in work:
+        a_hi, a_lo, b_hi, b_lo, kpad = ws[i]
+        assert kpad * esz % 16 == 0 and K[i] <= kpad < K[i] + 16 // esz
+        for off, rows in ((a_hi, M[i]), (b_hi, N[i])) + (((a_lo, M[i]), (b_lo, N[i]))
+                                                        if split else ()):
+            assert off % 256 == 0
+            spans.append((off, off + rows * kpad * esz))
+    spans.sort()
+    for (s0, e0), (s1, e1) in zip(spans, spans[1:]):
+        assert e0 <= s1, "workspace panels overlap"
+    assert not spans or spans[-1][1] <= used <= cap
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+@pytest.mark.parametrize("seed", [1, 2])
+def test_device_planner_replay_covers_everything(built_lib, mode, seed):
+    M, N, K = batch(seed * 7 + len(mode))
+    # the default bound (batch * 2 * max_dim * max_k) and the exact operand bound
+    elems = sum((m + n) * k for m, n, k in zip(M, N, K))
+    for bound in (0, elems):
+        items, jobs, ws, used, cap, err = fw_plan(M, N, K, 900, 700, mode, bound)
+        assert err == 0
+        check_plan(M, N, K, mode, items, jobs, ws, used, cap, [True] * len(M))
+
+
+def test_device_planner_replay_flags_out_of_bounds(built_lib):
+    M, N, K = [40, 950, 30, 8], [33, 20, 30, 8], [17, 20, 701, 8]
+    items, jobs, ws, used, cap, err = fw_plan(M, N, K, 900, 700, "tf32x3")
+    assert err == 1
+    check_plan(M, N, K, "tf32x3", items, jobs, ws, used, cap, [True, False, False, True])
+
+
+def test_device_planner_replay_operand_bound_too_small(built_lib):
+    M, N, K = batch(3)
+    elems = sum((m + n) * k for m, n, k in zip(M, N, K))
+    items, jobs, ws, used, cap, err = fw_plan(M, N, K, 900, 700, "tf32x3", elems // 4)
+    assert err == 2 and len(items) == 0 and len(jobs) == 0 and used > cap
+
+
+def test_device_planner_replay_prefers_pair_tiles_of_the_cost_table(built_lib):
+    """Large square matrices take the 256 x 256 pair tile; a tiny M with large
+    N is swapped so the 256-row side walks N."""
+    items, *_ = fw_plan([2048] * 4, [2048] * 4, [2048] * 4, 2048, 2048, "tf32x3")
+    assert len(items) == 4 * 8 * 8
+    items, *_ = fw_plan([3] * 8, [2048] * 8, [1024] * 8, 2048, 1024, "tf32x3")
+    tm_max = max(t[1] for t in items)
+    assert tm_max == 7  # 2048 / 256 tiles along the MMA's M side: the operands are swapped
