@@ -16,6 +16,7 @@
 // when a call needs more).
 #include <mutex>
 #include <unordered_map>
+#include <vector>
 
 #include "bgemm.h"
 #include "bgemm_internal.h"
@@ -39,6 +40,40 @@ struct FwScratch {
   TileItem* items;  // [cap_items]
 };
 
+// One matrix's tile configuration and bin (the same cost model as the host
+// planner); shared by fw_plan_kernel and its host replay.
+struct FwMat {
+  int bad;    // size negative or above max_dim: skipped
+  int cfg;    // -1: no output (M or N is 0, or skipped)
+  int tiles;
+  int bin;    // quarter-octave bin of the modelled tile time
+};
+
+__host__ __device__ inline FwMat fw_plan_matrix(int M, int N, int K, int max_dim,
+                                                const SimtCfg* cfgs, const TileCost* cost) {
+  FwMat r{};
+  r.bad = M < 0 || N < 0 || K < 0 || M > max_dim || N > max_dim;
+  r.cfg = -1;
+  if (!r.bad && M > 0 && N > 0) {
+    double bw = 0.0;
+    float btt = 0.f;
+    for (int c = kSimtNumCfgs - 1; c >= 0; --c) {
+      const long long t = (long long)((M + cfgs[c].bm - 1) / cfgs[c].bm) *
+                          ((N + cfgs[c].bn - 1) / cfgs[c].bn);
+      const float tt = cost[c].a_ns + cost[c].b_ns * (float)K;
+      const double w = (double)t * tt;
+      if (r.cfg < 0 || w < bw * 0.999) {
+        r.cfg = c;
+        r.tiles = (int)t;
+        bw = w;
+        btt = tt;
+      }
+    }
+    r.bin = min(kBins - 1, max(0, (int)(4.0f * log2f(fmaxf(btt, 1.0f)) - 24.0f)));
+  }
+  return r;
+}
+
 __global__ void fw_plan_kernel(const int* __restrict__ dM, const int* __restrict__ dN,
                                const int* __restrict__ dK, int batch, int max_dim,
                                FwScratch s) {
@@ -49,25 +84,11 @@ __global__ void fw_plan_kernel(const int* __restrict__ dM, const int* __restrict
   // per-matrix choice; the bin and offset are parked in mat_start for now
   for (int i = threadIdx.x; i < batch; i += blockDim.x) {
     const int M = dM[i], N = dN[i], K = dK[i];
-    const bool bad = M < 0 || N < 0 || K < 0 || M > max_dim || N > max_dim;
-    if (bad) atomicOr(s.err, 1);
-    int best = -1, bin = 0;
-    long long bt = 0;
-    float btt = 0.f;
-    if (!bad && M > 0 && N > 0) {
-      double bw = 0.0;
-      for (int c = kSimtNumCfgs - 1; c >= 0; --c) {
-        const long long t = (long long)((M + c_cfgs[c].bm - 1) / c_cfgs[c].bm) *
-                            ((N + c_cfgs[c].bn - 1) / c_cfgs[c].bn);
-        const float tt = c_cost[c].a_ns + c_cost[c].b_ns * (float)K;
-        const double w = (double)t * tt;
-        if (best < 0 || w < bw * 0.999) { best = c; bt = t; bw = w; btt = tt; }
-      }
-      bin = min(kBins - 1, max(0, (int)(4.0f * __log2f(fmaxf(btt, 1.0f)) - 24.0f)));
-    }
-    s.descs[i] = MatDesc{M, N, K, max(M, 1), max(K, 1), max(M, 1), best < 0 ? 0 : best,
-                         best < 0 ? 0 : bin};
-    s.mat_start[i] = best < 0 ? -1 : atomicAdd(&bin_tiles[bin], (int)bt);
+    const FwMat r = fw_plan_matrix(M, N, K, max_dim, c_cfgs, c_cost);
+    if (r.bad) atomicOr(s.err, 1);
+    s.descs[i] = MatDesc{M, N, K, max(M, 1), max(K, 1), max(M, 1), r.cfg < 0 ? 0 : r.cfg,
+                         r.cfg < 0 ? 0 : r.bin};
+    s.mat_start[i] = r.cfg < 0 ? -1 : atomicAdd(&bin_tiles[r.bin], r.tiles);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -275,4 +296,43 @@ extern "C" bgemm_status_t bgemm_framework_check_device(bgemm_stream_t stream) {
                      "a matrix size was negative or above max_dim; such matrices were skipped");
   }
   return BGEMM_SUCCESS;
+}
+
+// Host replay of fw_plan_kernel + fw_expand_kernel (tests without a GPU): the
+// same per-matrix choices, reserved in matrix order instead of by atomics.
+extern "C" int bgemm_debug_framework_plan(const int* M, const int* N, const int* K, int batch,
+                                          int max_dim, int* cfg_out, int* items_out,
+                                          int max_items, int* err) {
+  if (batch < 0 || !err || (batch > 0 && (!M || !N || !K))) return -1;
+  std::vector<FwMat> r(batch);
+  std::vector<int> start(batch, -1);
+  int bin_tiles[kBins] = {};
+  *err = 0;
+  for (int i = 0; i < batch; ++i) {
+    r[i] = fw_plan_matrix(M[i], N[i], K[i], max_dim, kSimtCfgs, kSimtCost);
+    if (r[i].bad) *err |= 1;
+    if (cfg_out) cfg_out[i] = r[i].cfg;
+    if (r[i].cfg >= 0) {
+      start[i] = bin_tiles[r[i].bin];
+      bin_tiles[r[i].bin] += r[i].tiles;
+    }
+  }
+  int bin_start[kBins], n = 0;
+  for (int b = kBins - 1; b >= 0; --b) {
+    bin_start[b] = n;
+    n += bin_tiles[b];
+  }
+  if (items_out && n > max_items) return -1;
+  for (int i = 0; items_out && i < batch; ++i) {
+    if (start[i] < 0) continue;
+    const int tmx = (M[i] + kSimtCfgs[r[i].cfg].bm - 1) / kSimtCfgs[r[i].cfg].bm;
+    const int tnx = (N[i] + kSimtCfgs[r[i].cfg].bn - 1) / kSimtCfgs[r[i].cfg].bn;
+    const int s0 = bin_start[r[i].bin] + start[i];
+    for (int t = 0; t < tmx * tnx; ++t) {
+      items_out[3 * (s0 + t)] = i;
+      items_out[3 * (s0 + t) + 1] = t % tmx;
+      items_out[3 * (s0 + t) + 2] = t / tmx;
+    }
+  }
+  return n;
 }

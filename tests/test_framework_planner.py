@@ -1,5 +1,6 @@
-"""Host replay of the device-side planner of bgemm_framework_gemm_mode
-(bgemm_debug_framework_tc_plan), without a GPU.
+"""Host replays of the device-side planners of bgemm_framework_gemm_mode
+(bgemm_debug_framework_tc_plan) and bgemm_framework_gemm
+(bgemm_debug_framework_plan), without a GPU.
 
 The same per-matrix decisions as fwtc_plan_kernel (tile configuration from the
 cost table, bins, strips, workspace panels), reserved in matrix order instead
@@ -152,3 +153,46 @@ def test_device_planner_replay_prefers_pair_tiles_of_the_cost_table(built_lib):
     items, *_ = fw_plan([3] * 8, [2048] * 8, [1024] * 8, 2048, 1024, "tf32x3")
     tm_max = max(t[1] for t in items)
     assert tm_max == 7  # 2048 / 256 tiles along the MMA's M side: the operands are swapped
+
+
+# ---- the SIMT entry (bgemm_framework_gemm) -------------------------------
+SIMT_CFGS = [(16, 16), (32, 32), (64, 32), (32, 64), (64, 64), (128, 64), (64, 128), (128, 128)]
+
+
+def fw_simt_plan(M, N, K, max_dim):
+    L = bg.lib()
+    n = len(M)
+    ia = lambda v: (ctypes.c_int * max(n, 1))(*v)
+    f = L.bgemm_debug_framework_plan
+    f.restype = ctypes.c_int
+    cfg = (ctypes.c_int * max(n, 1))()
+    err = ctypes.c_int()
+    cnt = f(ia(M), ia(N), ia(K), n, max_dim, cfg, None, 0, ctypes.byref(err))
+    assert cnt >= 0
+    items = (ctypes.c_int * max(3 * cnt, 1))()
+    assert f(ia(M), ia(N), ia(K), n, max_dim, cfg, items, cnt, ctypes.byref(err)) == cnt
+    return list(cfg)[:n], np.array(items[:3 * cnt]).reshape(-1, 3), err.value
+
+
+@pytest.mark.parametrize("seed", [4, 5, 6])
+def test_simt_device_planner_replay(built_lib, seed):
+    """Every tile of every in-bounds matrix once, a matrix's tiles adjacent;
+    out-of-bounds sizes flagged and skipped."""
+    M, N, K = batch(seed, n=120, max_dim=800, max_k=800)
+    M[6], N[7] = 900, 1000  # above max_dim: skipped and flagged
+    cfgs, items, err = fw_simt_plan(M, N, K, 800)
+    assert err == 1
+    seen, order = set(), []
+    for mat, tm, tn in items:
+        assert (mat, tm, tn) not in seen
+        seen.add((mat, tm, tn))
+        if not order or order[-1] != mat:
+            assert mat not in order
+            order.append(mat)
+    for i in range(len(M)):
+        got = {k for k in seen if k[0] == i}
+        if M[i] > 800 or N[i] > 800 or not (M[i] and N[i]):
+            assert cfgs[i] == -1 and not got
+            continue
+        bm, bn = SIMT_CFGS[cfgs[i]]
+        assert got == {(i, a, b) for a in range(-(-M[i] // bm)) for b in range(-(-N[i] // bn))}
