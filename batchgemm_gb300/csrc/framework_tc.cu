@@ -51,7 +51,7 @@ struct FwTcScratch {
   int* counters;     // GEMM queue counters (reset by the kernel)
   MatDesc* descs;    // [cap_batch]
   PackDesc* pdescs;  // [cap_batch]
-  int* bins;         // [cap_batch]
+  int* bins;         // [cap_batch] tile-time bin | K bin << 8
   int* mat_start;    // [cap_batch] first queue slot (-1: none)
   int* job_start;    // [cap_batch] first pre-pass strip (-1: none)
   TileItem* items;   // [cap_items]
