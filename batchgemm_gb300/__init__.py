@@ -16,6 +16,7 @@ __all__ = [
     "BgemmError", "MODES", "lib", "build", "sgemm_vbatched", "sgemm_vbatched_ex", "Plan",
     "plan_requirements", "max_requirements", "framework_gemm", "framework_gemm_mode",
     "framework_release", "framework_check_device", "device_info", "LIB_PATH",
+    "plan_cache_set_limit", "plan_cache_clear", "plan_cache_stats",
 ]
 
 PKG = os.path.dirname(os.path.abspath(__file__))
@@ -167,13 +168,19 @@ def lib() -> ctypes.CDLL:
     L.bgemm_status_string.restype = ctypes.c_char_p
     L.bgemm_device_info.argtypes = [ip, ip, ip]
     L.bgemm_version.restype = i
+    L.bgemm_plan_cache_set_limit.argtypes = [ctypes.c_size_t]
+    L.bgemm_plan_cache_clear.argtypes = []
+    ll = ctypes.POINTER(ctypes.c_longlong)
+    L.bgemm_debug_plan_cache_stats.argtypes = [ll] * 7
+    L.bgemm_debug_plan_cache_stats.restype = i
     for name in ("bgemm_sgemm_vbatched", "bgemm_plan_create", "bgemm_plan_create_ex",
                  "bgemm_plan_execute", "bgemm_plan_info", "bgemm_plan_check_device",
                  "bgemm_plan_destroy", "bgemm_framework_gemm", "bgemm_framework_check_device",
                  "bgemm_framework_gemm_noalloc", "bgemm_framework_gemm_mode", "bgemm_framework_release",
                  "bgemm_device_info",
                  "bgemm_plan_set_kernel_events", "bgemm_plan_requirements",
-                 "bgemm_plan_update", "bgemm_plan_capacity", "bgemm_sgemm_vbatched_ex"):
+                 "bgemm_plan_update", "bgemm_plan_capacity", "bgemm_sgemm_vbatched_ex",
+                 "bgemm_plan_cache_set_limit", "bgemm_plan_cache_clear"):
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -340,6 +347,24 @@ def framework_release() -> None:
 
 def framework_check_device(stream=None) -> None:
     _check(lib().bgemm_framework_check_device(_stream(stream)))
+
+
+def plan_cache_set_limit(nbytes: int) -> None:
+    """Device bytes the one-shot entries' cached plans may hold (0: default)."""
+    _check(lib().bgemm_plan_cache_set_limit(int(nbytes)))
+
+
+def plan_cache_clear() -> None:
+    """Free every evictable cached plan of the current device."""
+    _check(lib().bgemm_plan_cache_clear())
+
+
+def plan_cache_stats() -> dict:
+    """Counters of the plan cache on the current device."""
+    v = [ctypes.c_longlong() for _ in range(7)]
+    lib().bgemm_debug_plan_cache_stats(*[ctypes.byref(x) for x in v])
+    keys = ("entries", "bytes", "hits", "reorders", "misses", "evictions", "limit")
+    return {k: x.value for k, x in zip(keys, v)}
 
 
 def device_info() -> dict:

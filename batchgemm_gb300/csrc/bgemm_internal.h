@@ -18,6 +18,23 @@ struct MatDesc {
 constexpr int kTransAFlag = 1 << 28;
 constexpr int kTransBFlag = 1 << 29;
 
+// floor(4 * log2(x)) for x >= 1 (0 for smaller x), from the float's exponent
+// and mantissa bits with fixed quarter-octave edges, so that the host
+// replays of the device planners bin exactly as the device does (log2f of
+// the host C library and of CUDA may differ in the last bit).
+__host__ __device__ inline int quarter_octave(float x) {
+  if (!(x >= 1.0f)) return 0;
+  union {
+    float f;
+    uint32_t u;
+  } v;
+  v.f = x;
+  const int e = (int)((v.u >> 23) & 0xffu) - 127;
+  v.u = (v.u & 0x007fffffu) | 0x3f800000u;  // mantissa in [1, 2)
+  const int q = (v.f >= 1.18920712f) + (v.f >= 1.41421356f) + (v.f >= 1.68179283f);
+  return 4 * e + q;
+}
+
 // One work item of the largest-first tile queue (8 bytes).
 struct TileItem {
   int mat;

@@ -69,7 +69,7 @@ __host__ __device__ inline FwMat fw_plan_matrix(int M, int N, int K, int max_dim
         btt = tt;
       }
     }
-    r.bin = min(kBins - 1, max(0, (int)(4.0f * log2f(fmaxf(btt, 1.0f)) - 24.0f)));
+    r.bin = min(kBins - 1, max(0, quarter_octave(btt) - 24));
   }
   return r;
 }
@@ -156,8 +156,15 @@ extern "C" bgemm_status_t bgemm_framework_gemm(const int* dM, const int* dN, con
   bgemm_status_t st = device_facts(&df);
   if (st != BGEMM_SUCCESS) return st;
 
+  // worst-case queue: every matrix max_dim x max_dim in 16 x 16 tiles, 8
+  // bytes per item (batch = 1024, max_dim = 65536 would be 128 GB)
   const size_t per = (size_t)((max_dim + 15) / 16);
   const size_t need_items = (size_t)batch * per * per;
+  if (need_items > (size_t)INT32_MAX)
+    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 9, -1,
+                     "batch * ceil(max_dim/16)^2 = %zu queue items exceeds 2^31 - 1; pass a "
+                     "tighter max_dim",
+                     need_items);
   std::lock_guard<std::mutex> lk(g_fw_mu);
   FwContext& ctx = g_fw[df.device];
   if (!ctx.consts) {

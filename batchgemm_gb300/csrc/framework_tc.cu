@@ -101,7 +101,7 @@ __host__ __device__ inline FwTcMat fwtc_plan_matrix(int M, int N, int K, int max
     }
     if (best >= 0) {
       r.tiles = bt;
-      r.bin = min(kBins - 1, max(0, (int)(4.0f * log2f(fmaxf(btt, 1.0f)) - 24.0f)));
+      r.bin = min(kBins - 1, max(0, quarter_octave(btt) - 24));
     } else {
       r.nocfg = 1;
     }
@@ -114,7 +114,7 @@ __host__ __device__ inline FwTcMat fwtc_plan_matrix(int M, int N, int K, int max
   if (best >= 0 && K > 0) {
     r.a_bytes = ((unsigned long long)M * r.kpad * esz + 255) & ~255ull;
     r.b_bytes = ((unsigned long long)N * r.kpad * esz + 255) & ~255ull;
-    r.kbin = min(kBins - 1, (int)(4.0f * log2f((float)K)));
+    r.kbin = min(kBins - 1, quarter_octave((float)K));
     r.strips = cdiv(M, 32) + cdiv(N, 32);
   }
   return r;
@@ -430,7 +430,7 @@ extern "C" int bgemm_debug_framework_tc_plan(const int* M, const int* N, const i
                                              int mode, int* items_out, int max_items,
                                              int* jobs_out, int max_jobs, long long* ws_out,
                                              int* n_jobs, long long* ws_used,
-                                             long long* ws_capacity, int* err) {
+                                             long long* ws_capacity, int* err, int* cfg_out) {
   if (batch < 0 || mode < BGEMM_MODE_TF32 || mode > BGEMM_MODE_BF16X3 || !n_jobs || !ws_used ||
       !ws_capacity || !err || (batch > 0 && (!M || !N || !K)))
     return -1;
@@ -448,6 +448,7 @@ extern "C" int bgemm_debug_framework_tc_plan(const int* M, const int* N, const i
     r[i] = fwtc_plan_matrix(M[i], N[i], K[i], max_dim, max_k, mode, cost[mode - 1]);
     if (r[i].bad) *err |= 1;
     if (r[i].nocfg) *err |= 4;
+    if (cfg_out) cfg_out[i] = r[i].tiles ? r[i].desc.cfg : -1;
     if (r[i].tiles) {
       mat_start[i] = bin_tiles[r[i].bin];
       bin_tiles[r[i].bin] += r[i].tiles;
@@ -505,4 +506,23 @@ extern "C" int bgemm_debug_framework_tc_plan(const int* M, const int* N, const i
     }
   }
   return n_items;
+}
+
+// The cost-model entry (a + b*K ns per tile) the planners use for a mode's
+// configuration: the SIMT table (mode 0) or the tensor-core table as the
+// device planner completes it.
+extern "C" int bgemm_debug_tile_cost(int mode, int cfg, float* a_ns, float* b_ns) {
+  if (!a_ns || !b_ns || mode < BGEMM_MODE_SIMT_FP32 || mode > BGEMM_MODE_BF16X3) return -1;
+  if (mode == BGEMM_MODE_SIMT_FP32) {
+    if (cfg < 0 || cfg >= kSimtNumCfgs) return -1;
+    *a_ns = kSimtCost[cfg].a_ns;
+    *b_ns = kSimtCost[cfg].b_ns;
+    return 0;
+  }
+  if (cfg < 0 || cfg >= 16) return -1;
+  TileCost cost[3][16];
+  fwtc_cost_table(cost);
+  *a_ns = cost[mode - 1][cfg].a_ns;
+  *b_ns = cost[mode - 1][cfg].b_ns;
+  return 0;
 }

@@ -2,12 +2,10 @@
 // bgemm_framework_gemm for callers that cannot allocate device memory.
 //
 // Who needs it: code that must not call cudaMalloc/cudaFree once it is
-// running -- a stream being captured into a CUDA graph (allocation is not a
-// capturable operation and would break the capture), a real-time or
-// latency-critical loop where an allocation (which may synchronise the
-// device) is not allowed, a plug-in hosted by an application that owns the
-// device memory budget through its own pool, or a caller on a stream
-// callback thread where CUDA API calls that allocate are forbidden.
+// running -- a real-time or latency-bound loop where an allocation (which can
+// synchronise the whole device) is not allowed, or a plug-in hosted by an
+// application that owns the device memory budget through its own pool and
+// forbids allocations behind its back.
 //
 // The tile queue that the regular entry keeps in library-allocated memory
 // lives here in one file-scope __device__ array of fixed size, so no call
@@ -18,11 +16,16 @@
 // the process exits.
 //
 // Set-up: the first call on a device looks up the array's device address
-// (cudaGetSymbolAddress) with that device current; make that first call
-// before any stream capture begins.  All calls share the one array, so calls
-// whose work overlaps on the GPU (different streams, or different host
-// threads without ordering) race on it and must be serialised by the caller.
-// Each call clears the queue counters it needs before its kernels run.
+// (cudaGetSymbolAddress, return code checked) with that device current, and
+// the shared device planner uploads its cost tables to the device once
+// (cudaMemcpyToSymbol, a synchronous copy); make that first call before any
+// stream capture begins.  All calls share the one array and it keeps the last
+// call's contents, so calls whose work overlaps on the GPU (different
+// streams, or different host threads without ordering) race on it and must be
+// serialised by the caller.  Each call clears the queue counters and the
+// error word it needs before its kernels run.  With d_info == NULL the error
+// word is the array's own first int, which the next call clears and nothing
+// reads: out-of-range matrices are then skipped silently.
 #include <mutex>
 #include <unordered_map>
 

@@ -14,6 +14,7 @@
 //   - the six synchronous cudaMemcpy uploads (gemm.cu:57-77, 172-174) become
 //     one asynchronous copy of a packed descriptor block from pinned memory.
 #include <algorithm>
+#include <array>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -325,7 +326,7 @@ int debug_tc_plan(const int* M, const int* N, const int* K, int batch, int mode,
 
 static void free_plan_memory(bgemm_plan_s* p) {
   if (p->d_mem) cudaFree(p->d_mem);
-  for (int s = 0; s < 2; ++s) {
+  for (int s = 0; s < kStageBufs; ++s) {
     if (p->h_stage[s]) cudaFreeHost(p->h_stage[s]);
     if (p->ev_stage[s]) cudaEventDestroy(p->ev_stage[s]);
     p->h_stage[s] = nullptr;
@@ -386,7 +387,7 @@ static bgemm_status_t plan_alloc(bgemm_plan_s* p) {
   if (e != cudaSuccess)
     return set_error(BGEMM_ERROR_ALLOC, 0, -1, "device plan memory of %zu bytes: %s", p->mem_bytes,
                      cudaGetErrorString(e));
-  for (int s = 0; s < 2; ++s) {
+  for (int s = 0; s < kStageBufs; ++s) {
     e = cudaMallocHost(&p->h_stage[s], p->mem_bytes);
     if (e != cudaSuccess)
       return set_error(BGEMM_ERROR_ALLOC, 0, -1, "pinned staging of %zu bytes: %s", p->mem_bytes,
@@ -458,7 +459,7 @@ static bgemm_status_t plan_commit(bgemm_plan_s* p, BatchPlan& bp, bool first,
     if (e != cudaSuccess) return cuda_error(e, "staging event record");
     p->stage_used[s] = true;
   }
-  p->stage ^= 1;
+  p->stage = (p->stage + 1) % kStageBufs;
   p->info.batch = p->batch;
   p->info.num_tiles = p->n_items;
   std::memcpy(p->info.tile_config_hist, bp.hist, sizeof(bp.hist));
@@ -648,12 +649,44 @@ bgemm_status_t plan_destroy(bgemm_plan_t p) {
 }
 
 // ---------------------------------------------------------- plan cache ----
+// Plans of the one-shot entries, keyed by the batch's shape MULTISET: the
+// (M, N, K, lda, ldb, ldc) tuples sorted, plus device, mode and orientation.
+// The reference sorts its shape file offline by K and tile class before a
+// run (ROCm/data/sort.cpp:17-60) so that its dense grid meets similar tiles
+// together; here the planner orders the tile queue itself, so a batch's
+// order never matters for speed, and the cache makes it not matter for
+// planning either: the same shapes in another order reuse the plan through
+// plan_update (host planning + one upload; the device buffers, the
+// workspace and the kernels stay), and the result is bit-identical because
+// each matrix's tile choice depends only on its shape and on the multiset.
+//
+// The stream is not part of the key: an entry remembers the stream of its
+// last execute and an event recorded after it, and a call on another stream
+// first makes that stream wait for the event.  Entries are evicted least
+// recently used first when the cached device bytes would exceed the budget
+// (bgemm_plan_cache_set_limit; default a third of the device's memory), and
+// an allocation failure evicts every other entry of the device and retries
+// once.  An entry that was created or used while a stream was capturing is
+// pinned: a captured graph may replay it at any time, so it is never freed
+// or re-planned.
 namespace {
+struct CacheEntry {
+  bgemm_plan_t plan = nullptr;
+  int dev = 0;
+  std::string canon;          // device | mode | orientation | sorted tuples
+  std::vector<int> order;     // the committed batch's arrays M|N|K|lda|ldb|ldc
+  cudaStream_t stream = nullptr;  // stream of the last execute
+  cudaEvent_t done = nullptr;     // recorded after the last execute (outside capture)
+  bool done_valid = false;
+  bool pinned = false;        // used inside a stream capture
+  size_t bytes = 0;           // device bytes the plan owns
+};
 struct PlanCache {
   std::mutex mu;
-  std::list<std::string> lru;  // front = most recent
-  std::unordered_map<std::string, std::pair<bgemm_plan_t, std::list<std::string>::iterator>> map;
-  static constexpr size_t kMax = 32;
+  std::list<CacheEntry> lru;  // front = most recent
+  size_t limit = 0;           // 0: default of the device, set at first use
+  bool limit_set = false;
+  long long hits = 0, reorders = 0, misses = 0, evictions = 0;
   ~PlanCache() {
     // plans are intentionally leaked at process exit: the CUDA context may
     // already be gone, and freeing into it would fail.
@@ -663,64 +696,159 @@ PlanCache& cache() {
   static PlanCache* c = new PlanCache();
   return *c;
 }
+
+size_t cache_bytes(const PlanCache& c, int dev) {
+  size_t b = 0;
+  for (const CacheEntry& e : c.lru)
+    if (e.dev == dev) b += e.bytes;
+  return b;
+}
+
+size_t cache_limit(PlanCache& c) {
+  if (!c.limit_set) {
+    size_t free_b = 0, total_b = 0;
+    c.limit = cudaMemGetInfo(&free_b, &total_b) == cudaSuccess ? total_b / 3 : (size_t)8 << 30;
+    c.limit_set = true;
+  }
+  return c.limit;
+}
+
+void drop_entry(PlanCache& c, std::list<CacheEntry>::iterator it) {
+  plan_destroy(it->plan);  // cudaFree waits for work still using it
+  if (it->done) cudaEventDestroy(it->done);
+  c.lru.erase(it);
+  ++c.evictions;
+}
+
+// Evicts unpinned entries of `dev`, least recently used first, until `need`
+// more bytes fit under the limit (or nothing evictable is left).
+void make_room(PlanCache& c, int dev, size_t need, bool all) {
+  const size_t lim = cache_limit(c);
+  while (all || cache_bytes(c, dev) + need > lim) {
+    auto victim = c.lru.end();
+    for (auto it = c.lru.begin(); it != c.lru.end(); ++it)
+      if (it->dev == dev && !it->pinned) victim = it;  // the last match is the oldest
+    if (victim == c.lru.end()) return;
+    drop_entry(c, victim);
+  }
+}
+
+std::string canonical_key(const int* M, const int* N, const int* K, const int* lda,
+                          const int* ldb, const int* ldc, int batch, int dev, int mode,
+                          int orient) {
+  std::vector<std::array<int, 6>> t((size_t)batch);
+  for (int i = 0; i < batch; ++i) t[i] = {M[i], N[i], K[i], lda[i], ldb[i], ldc[i]};
+  std::sort(t.begin(), t.end());
+  std::string key(sizeof(int) * (3 + 6 * (size_t)batch), '\0');
+  int hdr[3] = {dev, mode, orient};
+  std::memcpy(&key[0], hdr, sizeof(hdr));
+  if (batch) std::memcpy(&key[sizeof(hdr)], t.data(), sizeof(int) * 6 * (size_t)batch);
+  return key;
+}
 }  // namespace
 
-bgemm_status_t cached_plan(bgemm_plan_t* out, const int* M, const int* N, const int* K,
-                           const int* lda, const int* ldb, const int* ldc, int batch, int mode,
-                           cudaStream_t stream, int layout = 0, int ta = 0, int tb = 0) {
+// Looks up (or builds) the plan of this batch and runs it on `stream`.
+bgemm_status_t cached_execute(const int* M, const int* N, const int* K, const int* lda,
+                              const int* ldb, const int* ldc, int batch, int mode,
+                              cudaStream_t stream, int layout, int ta, int tb, float alpha,
+                              const float* const* dA, const float* const* dB, float beta,
+                              float* const* dC) {
   int dev = 0;
   cudaGetDevice(&dev);
-  std::string key;
-  key.resize(sizeof(int) * (4 + 6 * (size_t)batch) + sizeof(void*));
-  char* k = &key[0];
-  int hdr[4] = {dev, mode, batch, layout | (ta << 1) | (tb << 2)};
-  std::memcpy(k, hdr, sizeof(hdr));
-  k += sizeof(hdr);
-  void* sp = stream;
-  std::memcpy(k, &sp, sizeof(void*));
-  k += sizeof(void*);
-  for (const int* a : {M, N, K, lda, ldb, ldc}) {
-    std::memcpy(k, a, sizeof(int) * (size_t)batch);
-    k += sizeof(int) * (size_t)batch;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(stream, &cs);
+  const bool capturing = cs != cudaStreamCaptureStatusNone;
+  const int orient = layout | (ta << 1) | (tb << 2);
+  std::string canon = canonical_key(M, N, K, lda, ldb, ldc, batch, dev, mode, orient);
+  std::vector<int> order(6 * (size_t)batch);
+  {
+    int* o = order.data();
+    for (const int* a : {M, N, K, lda, ldb, ldc}) {
+      if (batch) std::memcpy(o, a, sizeof(int) * (size_t)batch);
+      o += batch;
+    }
   }
   PlanCache& c = cache();
   std::lock_guard<std::mutex> lk(c.mu);
-  auto it = c.map.find(key);
-  if (it != c.map.end()) {
-    c.lru.splice(c.lru.begin(), c.lru, it->second.second);
-    *out = it->second.first;
-    return BGEMM_SUCCESS;
-  }
-  bgemm_plan_t p = nullptr;
-  bgemm_plan_options_t opt = default_options();
-  opt.layout = layout;
-  opt.trans_a = ta;
-  opt.trans_b = tb;
-  bgemm_status_t st = plan_create(&p, M, N, K, lda, ldb, ldc, batch, mode, stream, &opt);
-  if (st != BGEMM_SUCCESS) return st;
-  if (c.map.size() >= PlanCache::kMax) {
-    const std::string& victim = c.lru.back();
-    auto vit = c.map.find(victim);
-    if (vit != c.map.end()) {
-      plan_destroy(vit->second.first);  // cudaFree waits for in-flight work
-      c.map.erase(vit);
+  // 1. an entry holding this exact order; 2. one holding another order that
+  // may be re-planned (outside a capture, not pinned)
+  auto exact = c.lru.end(), other = c.lru.end();
+  for (auto it = c.lru.begin(); it != c.lru.end(); ++it) {
+    if (it->dev != dev || it->canon != canon) continue;
+    const bool stream_ok = it->stream == stream || !capturing;
+    if (it->order == order && stream_ok) {
+      exact = it;
+      break;
     }
-    c.lru.pop_back();
+    if (other == c.lru.end() && !capturing && !it->pinned) other = it;
   }
-  c.lru.push_front(key);
-  c.map.emplace(key, std::make_pair(p, c.lru.begin()));
-  *out = p;
-  return BGEMM_SUCCESS;
+  auto ent = exact != c.lru.end() ? exact : other;
+  bgemm_status_t st = BGEMM_SUCCESS;
+  if (ent != c.lru.end()) {
+    if (ent->stream != stream && ent->done_valid) {
+      cudaError_t e = cudaStreamWaitEvent(stream, ent->done, 0);
+      if (e != cudaSuccess) return cuda_error(e, "ordering a cached plan across streams");
+    }
+    if (ent == other) {
+      st = plan_update(ent->plan, M, N, K, lda, ldb, ldc, batch, stream);
+      if (st == BGEMM_SUCCESS) {
+        ent->order.swap(order);
+        ++c.reorders;
+      } else {
+        clear_error();
+        ent = c.lru.end();  // not re-plannable: build a plan of its own below
+      }
+    } else {
+      ++c.hits;
+    }
+    if (ent != c.lru.end()) c.lru.splice(c.lru.begin(), c.lru, ent);
+  }
+  if (ent == c.lru.end()) {
+    ++c.misses;
+    bgemm_plan_options_t opt = default_options();
+    opt.layout = layout;
+    opt.trans_a = ta;
+    opt.trans_b = tb;
+    if (!capturing) {
+      // room for the new plan before it allocates
+      bgemm_plan_requirements_t req{};
+      if (plan_requirements(M, N, K, lda, ldb, ldc, batch, mode, &opt, &req) == BGEMM_SUCCESS)
+        make_room(c, dev,
+                  req.workspace_bytes + 32 * (size_t)req.batch + 8 * (size_t)req.tiles + 65536,
+                  false);
+    }
+    bgemm_plan_t p = nullptr;
+    st = plan_create(&p, M, N, K, lda, ldb, ldc, batch, mode, stream, &opt);
+    if (st == BGEMM_ERROR_ALLOC && !capturing) {
+      make_room(c, dev, 0, true);
+      st = plan_create(&p, M, N, K, lda, ldb, ldc, batch, mode, stream, &opt);
+    }
+    if (st != BGEMM_SUCCESS) return st;
+    CacheEntry e;
+    e.plan = p;
+    e.dev = dev;
+    e.canon.swap(canon);
+    e.order.swap(order);
+    e.bytes = p->info.device_bytes;
+    cudaEventCreateWithFlags(&e.done, cudaEventDisableTiming);
+    c.lru.push_front(std::move(e));
+    ent = c.lru.begin();
+  }
+  st = plan_execute(ent->plan, alpha, dA, dB, beta, dC, stream);
+  ent->stream = stream;
+  if (capturing) {
+    ent->pinned = true;
+    ent->done_valid = false;
+  } else if (ent->done) {
+    ent->done_valid = cudaEventRecord(ent->done, stream) == cudaSuccess;
+  }
+  return st;
 }
 
 }  // namespace bgemm
 
 // ================================================================ C ABI ====
 using namespace bgemm;
-
-extern "C" {
-
-}  // extern "C"
 
 namespace bgemm {
 // Shared body of the one-shot entries; arg[] holds the caller's argument
@@ -739,10 +867,8 @@ static bgemm_status_t vbatched(int layout, int ta, int tb, const int* M, const i
   if (!dA) return set_error(BGEMM_ERROR_INVALID_VALUE, arg[3], -1, "dA is NULL");
   if (!dB) return set_error(BGEMM_ERROR_INVALID_VALUE, arg[5], -1, "dB is NULL");
   if (!dC) return set_error(BGEMM_ERROR_INVALID_VALUE, arg[7], -1, "dC is NULL");
-  bgemm_plan_t p = nullptr;
-  st = cached_plan(&p, M, N, K, lda, ldb, ldc, batch, mode, stream, layout, ta, tb);
-  if (st != BGEMM_SUCCESS) return st;
-  st = plan_execute(p, alpha, dA, dB, beta, dC, stream);
+  st = cached_execute(M, N, K, lda, ldb, ldc, batch, mode, stream, layout, ta, tb, alpha, dA,
+                      dB, beta, dC);
   if (st == BGEMM_ERROR_INVALID_VALUE && t_err_arg > 0) {
     // plan_execute numbers its own arguments; map them to this entry point
     const int map[7] = {0, 0, 0, arg[3], arg[5], 0, arg[7]};
@@ -902,6 +1028,51 @@ bgemm_status_t bgemm_device_info(int* num_sms, int* simt_ctas_per_sm, int* tc_ct
 }
 
 int bgemm_version(void) { return 100; }
+
+bgemm_status_t bgemm_plan_cache_set_limit(size_t bytes) {
+  clear_error();
+  PlanCache& c = cache();
+  std::lock_guard<std::mutex> lk(c.mu);
+  if (bytes == 0) {
+    c.limit_set = false;  // back to the default, taken at the next use
+  } else {
+    c.limit = bytes;
+    c.limit_set = true;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) make_room(c, dev, 0, false);
+  return BGEMM_SUCCESS;
+}
+
+bgemm_status_t bgemm_plan_cache_clear(void) {
+  clear_error();
+  PlanCache& c = cache();
+  std::lock_guard<std::mutex> lk(c.mu);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+  make_room(c, dev, 0, true);
+  return BGEMM_SUCCESS;
+}
+
+int bgemm_debug_plan_cache_stats(long long* entries, long long* bytes, long long* hits,
+                                 long long* reorders, long long* misses, long long* evictions,
+                                 long long* limit) {
+  PlanCache& c = cache();
+  std::lock_guard<std::mutex> lk(c.mu);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  long long n = 0;
+  for (const CacheEntry& e : c.lru) n += e.dev == dev;
+  if (entries) *entries = n;
+  if (bytes) *bytes = (long long)cache_bytes(c, dev);
+  if (hits) *hits = c.hits;
+  if (reorders) *reorders = c.reorders;
+  if (misses) *misses = c.misses;
+  if (evictions) *evictions = c.evictions;
+  if (limit) *limit = c.limit_set ? (long long)c.limit : 0;
+  return 0;
+}
 
 int bgemm_debug_compare_tensor_maps(void* plan, void* stream, int* n_maps, int* n_diff,
                                     int* first_byte) {

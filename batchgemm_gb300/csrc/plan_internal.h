@@ -37,6 +37,9 @@ constexpr int kTcNumCfgs = 16;
 constexpr int kHdrItems = 16;
 constexpr int kHdrJobs = 17;
 constexpr size_t kHdrBytes = 256;
+// Pinned staging buffers of a plan's uploads, used in turn: an update waits
+// only for the upload kStageBufs updates back to have been consumed.
+constexpr int kStageBufs = 3;
 
 // Host result of planning one batch, before anything is written to the
 // plan's buffers (an update that does not fit leaves the plan untouched).
@@ -65,9 +68,9 @@ struct bgemm_plan_s {
   bool row_major = false;
   int aux_trans = 0;               // kTransAFlag / kTransBFlag of the planned product
   void* d_mem = nullptr;           // header | descs[cap] | items[cap]
-  void* h_stage[2] = {nullptr, nullptr};  // double-buffered pinned staging, same layout
-  cudaEvent_t ev_stage[2] = {nullptr, nullptr};  // upload from h_stage[i] consumed
-  bool stage_used[2] = {false, false};
+  void* h_stage[bgemm::kStageBufs] = {};      // ring of pinned staging, same layout
+  cudaEvent_t ev_stage[bgemm::kStageBufs] = {};  // upload from h_stage[i] consumed
+  bool stage_used[bgemm::kStageBufs] = {};
   int stage = 0;                   // staging buffer of the next upload
   bool staged_in_capture = false;  // created during a stream capture (no updates)
   size_t off_descs = 0, off_items = 0, mem_bytes = 0;

@@ -9,7 +9,7 @@
 //
 // Each item is one BM x BN output tile of one matrix.  256 threads form a
 // 16 x 16 grid; each owns a TM x TN register tile.  Operands stream through a
-// 4-stage cp.async ring of BK = 8 k-slices:
+// 4-stage cp.async ring of BK = 16 k-slices:
 //   A slice: [k][BM]     (column of A, 16-byte cp.async when lda % 4 == 0 and
 //                         A is 16-byte aligned, 4-byte otherwise)
 //   B slice: [k][BN + 4] (transposed on the way in by 4-byte cp.async; the

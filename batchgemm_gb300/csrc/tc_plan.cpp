@@ -30,7 +30,7 @@ struct TcPlan {
   size_t cap_ws = 0;
   void* d_ws = nullptr;      // split operands
   void* d_mem = nullptr;     // templates | tensor maps | pack descs | jobs | error word
-  void* h_stage[2] = {nullptr, nullptr};  // pinned staging, same layout as d_mem
+  void* h_stage[kStageBufs] = {};  // pinned staging ring, same layout as d_mem
   size_t off_tm = 0, off_pd = 0, off_jobs = 0, off_err = 0, mem_bytes = 0;
   CUtensorMap* d_templ = nullptr;
   CUtensorMap* d_tmaps = nullptr;
@@ -276,11 +276,12 @@ bgemm_status_t tc_alloc(bgemm_plan_s* p) {
     return set_error(BGEMM_ERROR_ALLOC, 0, -1, "split-operand workspace of %zu bytes: %s",
                      t->cap_ws, cudaGetErrorString(e));
   e = cudaMalloc(&t->d_mem, t->mem_bytes);
-  for (int s = 0; s < 2 && e == cudaSuccess; ++s) e = cudaMallocHost(&t->h_stage[s], t->mem_bytes);
+  for (int s = 0; s < kStageBufs && e == cudaSuccess; ++s)
+    e = cudaMallocHost(&t->h_stage[s], t->mem_bytes);
   if (e != cudaSuccess)
     return set_error(BGEMM_ERROR_ALLOC, 0, -1, "tensor-core plan memory: %s",
                      cudaGetErrorString(e));
-  for (int s = 0; s < 2; ++s) std::memset(t->h_stage[s], 0, t->mem_bytes);
+  for (int s = 0; s < kStageBufs; ++s) std::memset(t->h_stage[s], 0, t->mem_bytes);
   if (!tc_encode_templates(t->kind, t->d_ws, static_cast<CUtensorMap*>(t->h_stage[0])))
     return set_error(BGEMM_ERROR_INTERNAL, 0, -1, "template tensor map encoding failed");
   char* dm = static_cast<char*>(t->d_mem);

@@ -202,9 +202,12 @@ def cpu_sample(w, budget_s=15.0, threads=None):
 
 
 # ---------------------------------------------------------------- GPU leg --
-def fp64_sampled_error(db, per_matrix=4, seed=0, C0=None, beta=0.0, alpha=1.0):
+def fp64_sampled_error(db, per_matrix=4, seed=0, C0=None, beta=0.0, alpha=1.0,
+                       samples=False):
     """Normalised error |c - c64| / (|alpha| sum|a b| + |beta c0|) on sampled
-    entries, FP64 on the GPU (C0: the C buffer before the step, when beta != 0)."""
+    entries, FP64 on the GPU (C0: the C buffer before the step, when beta != 0).
+    Returns (max, mean, count), or with samples=True (errors, K of each
+    sample) as numpy arrays."""
     import torch
     rng = np.random.default_rng(seed)
     idx_m, idx_n, mats = [], [], []
@@ -215,7 +218,7 @@ def fp64_sampled_error(db, per_matrix=4, seed=0, C0=None, beta=0.0, alpha=1.0):
                 idx_m.append(int(rng.integers(0, db.M[i])))
                 idx_n.append(int(rng.integers(0, db.N[i])))
     if not mats:
-        return 0.0, 0.0, 0
+        return (np.zeros(0), np.zeros(0)) if samples else (0.0, 0.0, 0)
     kmax = max(db.K[i] for i in mats)
     S = len(mats)
     dev = db.A.device
@@ -245,6 +248,8 @@ def fp64_sampled_error(db, per_matrix=4, seed=0, C0=None, beta=0.0, alpha=1.0):
             absb = absb + c0.abs()
         errs.append(((c - exact).abs() / absb.clamp_min(1e-300)).cpu())
     e = torch.cat(errs)
+    if samples:
+        return e.numpy(), np.array([db.K[i] for i in mats], dtype=np.float64)
     return float(e.max()), float(e.mean()), S
 
 
@@ -333,6 +338,11 @@ def gpu_leg(args, rank, world, local):
         return plan, info, ms, (clk.summary() if clk else None)
 
     out = {}
+    if args.mode in ("tf32", "tf32x3"):
+        # the TF32 tensor rate of this GPU, measured before the timed region
+        from batchgemm_gb300 import peaks as peaks_mod
+        out["tf32_peak"] = peaks_mod.tf32_burst()
+        torch.cuda.empty_cache()
     plan, info, ms, clocks = time_mode(args.mode, args.steps, args.warmup, sample_clocks=True)
     value, ms_max = whole_job_tflops(flops, ms, world, dev)
     err_max, err_mean, nsamp = one_step_error(plan)
@@ -431,20 +441,37 @@ def gpu_leg(args, rank, world, local):
                            "peak_source": "SMs x 128 FP32 lanes x 2 x max SM clock (device "
                                           "properties; MEASURED_PEAKS.json has no FP32 figure)"}
     else:
-        bf16 = peaks.get("bf16_tflops", 1900.0)
-        src = "of measured" if "bf16_tflops" in peaks else "of fallback"
         mult = 3.0 if mode in ("tf32x3", "bf16x3") else 1.0
-        pipe_peak = bf16 if mode == "bf16x3" else bf16 / 2.0
+        if mode == "bf16x3":
+            pipe_peak = peaks.get("bf16_tflops", 1900.0)
+            src = ("of measured bf16 dense (MEASURED_PEAKS.json, cuBLAS bf16 8192^3, burst)"
+                   if "bf16_tflops" in peaks else "of fallback bf16 dense 1.9 PFLOP/s")
+        else:
+            pipe_peak = out["tf32_peak"]
+            src = ("of measured TF32 dense: cuBLAS TF32 GEMM 8192^3 (torch.matmul, FP32 "
+                   "operands, TF32 allowed), best of 10 by CUDA events, measured in this run "
+                   "before the timed region (batchgemm_gb300.peaks.tf32_burst)")
         ach = mult * flops / (kms * 1e-3) / 1e12
+        step_ms = out["ms"]
+        pre_ms = step_ms - kms
+        pre_traffic = ncu_traffic(mode + "_pre_pass", w.name)
         out["roofline"] = {"bound": "tensor", "achieved": round(ach, 2),
                            "peak": round(pipe_peak, 1), "unit": "TFLOP/s",
                            "frac": round(ach / pipe_peak, 4), "traffic": traffic,
                            "kernel": "tc2_gemm_kernel / tc_gemm_kernel", "kernel_ms": round(kms, 4),
-                           "pre_pass_ms": round(out["ms"] - kms, 4),
+                           "pre_pass_ms": round(pre_ms, 4),
                            "algorithmic_flops_per_launch": mult * flops,
-                           "peak_source": "%s bf16 dense%s%s" % (
-                               src, "" if mode == "bf16x3" else " / 2 (TF32 rate)",
-                               "; achieved counts the 3 tensor products" if mult > 1 else "")}
+                           "peak_source": src + ("; achieved counts the 3 tensor products"
+                                                 if mult > 1 else ""),
+                           # the whole step (pre-pass + GEMM) against the same pipe:
+                           # useful flops over (peak / products)
+                           "step_frac": round(mult * flops / (step_ms * 1e-3) / 1e12 / pipe_peak,
+                                              4),
+                           "step_dram_bytes": (traffic + pre_traffic
+                                               if traffic and pre_traffic else None),
+                           "pre_pass_traffic": pre_traffic}
+        if mode != "bf16x3" and "bf16_tflops" in peaks:
+            out["roofline"]["bf16_measured_tflops"] = peaks["bf16_tflops"]
 
     # end to end through the one-shot C-ABI call with host buffers.  Every
     # step copies its inputs in from pinned host memory, runs
@@ -590,8 +617,8 @@ def stream_leg(args, dev, s):
         graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(graph, stream=s):
             plan.execute(1.0, pA, pB, 1.0, pC, stream=s)
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-               for _ in range(nb)]
+        mk = lambda: torch.cuda.Event(enable_timing=True)
+        evs = [(mk(), mk(), mk()) for _ in range(nb)]
         host_ms = []
         torch.cuda.synchronize(dev)
         with torch.cuda.stream(s):
@@ -601,12 +628,14 @@ def stream_leg(args, dev, s):
                 t0 = time.perf_counter()
                 plan.update(*arrs[b], stream=s)
                 host_ms.append((time.perf_counter() - t0) * 1e3)
+                evs[b][1].record(s)  # uploads enqueued: the GPU part starts here
                 graph.replay()
-                evs[b][1].record(s)
+                evs[b][2].record(s)
         s.synchronize()
         plan.check_device(stream=s)
-        lat = sorted(a.elapsed_time(c) for a, c in evs)
-        total_ms = evs[0][0].elapsed_time(evs[-1][1])
+        lat = sorted(a.elapsed_time(c) for a, _, c in evs)
+        gpu = sorted(r.elapsed_time(c) for _, r, c in evs)
+        total_ms = evs[0][0].elapsed_time(evs[-1][2])
         # accuracy of the last batch, run again from a snapshot of C
         b = nb - 1
         w = bs[b]
@@ -621,36 +650,136 @@ def stream_leg(args, dev, s):
             ldb=[max(1, k) for k in w.K], ldc=[max(1, m) for m in w.M], offA=offs["A"][b],
             offB=offs["B"][b], offC=offs["C"][b], A=pools["A"], B=pools["B"], C=pools["C"])
         e_max, e_mean, n_s = fp64_sampled_error(view, per_matrix=2, C0=C0, beta=1.0)
+        # and of ten more batches (each from a snapshot of C)
+        errs = [(e_mean, e_max, n_s)]
+        for b in range(max(0, nb - 11), nb - 1):
+            w = bs[b]
+            C0.copy_(pools["C"])
+            with torch.cuda.stream(s):
+                ptr_dev.copy_(ptr_host[b], non_blocking=True)
+                plan.update(*arrs[b], stream=s)
+                graph.replay()
+            s.synchronize()
+            view = types.SimpleNamespace(
+                batch=w.batch, M=w.M, N=w.N, K=w.K, lda=[max(1, m) for m in w.M],
+                ldb=[max(1, k) for k in w.K], ldc=[max(1, m) for m in w.M], offA=offs["A"][b],
+                offB=offs["B"][b], offC=offs["C"][b], A=pools["A"], B=pools["B"], C=pools["C"])
+            mx, mn, n_b = fp64_sampled_error(view, per_matrix=2, C0=C0, beta=1.0, seed=b)
+            errs.append((mn, mx, n_b))
+        n_all = sum(e[2] for e in errs)
+        err_batches = {"batches": len(errs), "samples": n_all,
+                       "mean": sum(e[0] * e[2] for e in errs) / max(n_all, 1),
+                       "max": max(e[1] for e in errs)}
         del C0, graph
         info = plan.info()
         plan.close()
         pct = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]
+        gpct = lambda q: gpu[min(len(gpu) - 1, int(round(q * (len(gpu) - 1))))]
         return {"tflops": round(sum(flops) / (total_ms * 1e-3) / 1e12, 3),
                 "total_ms": round(total_ms, 2),
                 "latency_ms_p50": round(pct(0.50), 4), "latency_ms_p99": round(pct(0.99), 4),
                 "latency_ms_max": round(lat[-1], 4),
+                "gpu_replay_ms_p50": round(gpct(0.50), 4),
+                "gpu_replay_ms_p99": round(gpct(0.99), 4),
+                "gpu_replay_ms_sum": round(sum(gpu), 2),
                 "host_update_ms_p50": round(statistics.median(host_ms), 4),
                 "host_requirements_ms_mean": round(req_ms, 4),
                 "kernels_per_batch": info["kernels_per_execute"] + (0 if mode == "simt" else 1),
                 "capacity": cap,
-                "err_vs_fp64_last_batch": {"max": e_max, "mean": e_mean, "samples": n_s}}
+                "err_vs_fp64_last_batch": {"max": e_max, "mean": e_mean, "samples": n_s},
+                "err_vs_fp64_batches": err_batches}
+
+    def run_device_sizes(mode):
+        """The same stream through bgemm_framework_gemm_mode: per batch only the
+        size and pointer arrays are copied to the device (padded to the
+        largest batch with empty matrices) and one captured call replays; the
+        tile choice, queue, split operands and tensor maps are built on the
+        device, so there is no host planning at all."""
+        cap = max(w.batch for w in bs)
+        sz_host = torch.zeros((nb, 3, cap), dtype=torch.int32, pin_memory=True)
+        for b, w in enumerate(bs):
+            for j, v in enumerate((w.M, w.N, w.K)):
+                sz_host[b, j, :w.batch] = torch.tensor(v, dtype=torch.int32)
+        sz_dev = torch.zeros((3, cap), dtype=torch.int32, device=dev)
+        ptr_dev = torch.zeros((3, cap_batch), dtype=torch.int64, device=dev)
+        max_dim = max(max(max(w.M), max(w.N)) for w in bs)
+        max_k = max(max(w.K) for w in bs)
+        elems = max(sum((m + n) * k for m, n, k in zip(w.M, w.N, w.K)) for w in bs)
+        fw = (sz_dev[0].data_ptr(), sz_dev[1].data_ptr(), sz_dev[2].data_ptr(),
+              ptr_dev[0].data_ptr(), ptr_dev[1].data_ptr(), ptr_dev[2].data_ptr(), cap,
+              max_dim, max_k)
+
+        def upload(b):
+            sz_dev.copy_(sz_host[b], non_blocking=True)
+            ptr_dev.copy_(ptr_host[b], non_blocking=True)
+
+        with torch.cuda.stream(s):
+            for b in range(3):
+                upload(b)
+                bg.framework_gemm_mode(*fw, mode=mode, stream=s, max_operand_elems=elems)
+        s.synchronize()
+        bg.framework_check_device(s)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=s):
+            bg.framework_gemm_mode(*fw, mode=mode, stream=s, max_operand_elems=elems)
+        mk = lambda: torch.cuda.Event(enable_timing=True)
+        evs = [(mk(), mk(), mk()) for _ in range(nb)]
+        torch.cuda.synchronize(dev)
+        with torch.cuda.stream(s):
+            for b in range(nb):
+                evs[b][0].record(s)
+                upload(b)
+                evs[b][1].record(s)
+                graph.replay()
+                evs[b][2].record(s)
+        s.synchronize()
+        bg.framework_check_device(s)
+        lat = sorted(a.elapsed_time(c) for a, _, c in evs)
+        gpu = sorted(r.elapsed_time(c) for _, r, c in evs)
+        total_ms = evs[0][0].elapsed_time(evs[-1][2])
+        del graph
+        bg.framework_release()
+        pct = lambda v, q: v[min(len(v) - 1, int(round(q * (len(v) - 1))))]
+        return {"api": "bgemm_framework_gemm_mode (device size arrays, C += A B)",
+                "tflops": round(sum(flops) / (total_ms * 1e-3) / 1e12, 3),
+                "total_ms": round(total_ms, 2),
+                "latency_ms_p50": round(pct(lat, 0.5), 4),
+                "latency_ms_p99": round(pct(lat, 0.99), 4),
+                "gpu_replay_ms_p50": round(pct(gpu, 0.5), 4),
+                "gpu_replay_ms_p99": round(pct(gpu, 0.99), 4),
+                "host_planning_ms": 0.0,
+                "bounds": {"batch": cap, "max_dim": max_dim, "max_k": max_k,
+                           "max_operand_elems": elems}}
 
     out = {"workload": "stream_%d: %d successive batches, U{64..1024} matrices each, M, N, K "
                        "log-uniform in [1, 4096], U[-1,1], alpha = beta = 1" % (nb, nb),
            "useful_tflop_total": round(sum(flops) / 1e12, 3),
            "per_batch_gflop_p50": round(statistics.median(flops) / 1e9, 2),
-           "timing": "per batch: CUDA events around pointer upload + bgemm_plan_update + "
-                     "graph replay on the launching stream; aggregate = all batches / first "
-                     "start to last stop; operands rotate through pools twice the largest "
-                     "batch (no L2 reuse between batches)"}
+           "timing": "per batch: CUDA events on the launching stream before the pointer "
+                     "upload, after bgemm_plan_update's uploads (gpu_replay = from there to "
+                     "the end of the graph replay: GPU work only) and after the replay "
+                     "(latency); host_update = wall time of bgemm_plan_update on the host "
+                     "(planning plus any wait for a staging buffer), host_requirements = "
+                     "host planning alone; aggregate = all batches / first start to last "
+                     "stop; operands rotate through pools twice the largest batch (no L2 "
+                     "reuse between batches)"}
     for mode in (args.mode, "simt") if args.mode != "simt" else ("simt",):
         try:
             out[mode] = run(mode)
         except bg.BgemmError as e:
             out[mode] = {"unavailable": e.message}
+        torch.cuda.empty_cache()
+        try:
+            out["device_sizes_" + mode] = run_device_sizes(mode)
+        except bg.BgemmError as e:
+            out["device_sizes_" + mode] = {"unavailable": e.message}
+        torch.cuda.empty_cache()
     if args.mode != "simt" and "tflops" in out.get(args.mode, {}) and \
             "tflops" in out.get("simt", {}):
         out["ratio_vs_simt"] = round(out[args.mode]["tflops"] / out["simt"]["tflops"], 3)
+        a, b = out.get("device_sizes_" + args.mode, {}), out.get("device_sizes_simt", {})
+        if "tflops" in a and "tflops" in b:
+            out["ratio_vs_simt_device_sizes"] = round(a["tflops"] / b["tflops"], 3)
     for key in list(pools):
         del pools[key]
     return out
@@ -678,8 +807,10 @@ def main():
         vals = []
         desc = ""
         cores = 0
+        # warm-up: the same loop, untimed, on a short sample (thread pool,
+        # page-in of the oracle library and of the generated operands)
         for _ in range(args.warmup):
-            pass
+            cpu_sample(w, budget_s=0.5)
         steps = max(1, min(args.steps, 3))
         for _ in range(steps):
             v, cores, desc = cpu_sample(w, budget_s=8.0)

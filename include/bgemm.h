@@ -136,8 +136,19 @@ typedef struct bgemm_plan_options {
  * M, N, K, lda, ldb, ldc: HOST arrays [batch]; dA, dB, dC: DEVICE arrays
  * [batch] of device pointers.  Requirements: M,N,K >= 0, lda >= max(1,M),
  * ldb >= max(1,K), ldc >= max(1,M); pointers of empty matrices are not read.
- * Plans are cached per (shapes, mode, stream); a cache miss builds and
- * uploads a plan on `stream` without blocking on the GPU. */
+ * Plans are cached per shape multiset (device, mode and orientation, and
+ * the batch's (M, N, K, lda, ldb, ldc) tuples in any order -- the
+ * counterpart of the reference's offline shape sort, ROCm/data/sort.cpp:
+ * 17-60): the same shapes in another order re-plan into the cached plan
+ * (host planning + one upload, no allocation) and give bit-identical
+ * results per matrix.  A cached plan used on another stream first waits
+ * for its previous use.  A cache miss builds and uploads a plan on `stream`
+ * without blocking on the GPU; it first evicts least recently used plans
+ * so that the cached device bytes stay under the limit of
+ * bgemm_plan_cache_set_limit, and on an allocation failure it evicts every
+ * other plan of the device and retries once.  Plans created or used while
+ * `stream` is capturing are never evicted or re-planned (a graph may replay
+ * them). */
 bgemm_status_t bgemm_sgemm_vbatched(const int* M, const int* N, const int* K,
                                     float alpha, const float* const* dA,
                                     const int* lda, const float* const* dB,
@@ -199,9 +210,9 @@ bgemm_status_t bgemm_plan_info(bgemm_plan_t plan, bgemm_plan_info_t* info);
  * the new batch's pointers where the graph reads them).  The update is
  * stream-ordered: executes enqueued on `stream` before it see the previous
  * batch, later ones the new batch; work on other streams must be ordered by
- * the caller.  Host staging is double-buffered, so the call blocks only
- * until the upload of the update before the previous one has been consumed;
- * it must not be called while `stream` is capturing.  A batch beyond the
+ * the caller.  Host staging is a ring of three pinned buffers, so the call
+ * blocks only until the upload of the third update back has been consumed
+ * by the GPU; it must not be called while `stream` is capturing.  A batch beyond the
  * plan's capacity fails with BGEMM_ERROR_NOT_SUPPORTED and leaves the plan
  * holding its previous batch. */
 bgemm_status_t bgemm_plan_requirements(const int* M, const int* N, const int* K,
@@ -286,24 +297,39 @@ bgemm_status_t bgemm_framework_release(void);
 /* --- allocation-free variant of bgemm_framework_gemm ----------------------
  * No counterpart in the reference.  Same arguments and result as
  * bgemm_framework_gemm (device size arrays, C_i += A_i*B_i, FP32 SIMT,
- * bit-exact), for callers that cannot allocate device memory while they run:
- * a stream under CUDA-graph capture, a real-time loop, a plug-in whose host
- * application owns the memory budget.  The tile queue lives in a fixed
+ * bit-exact), for callers that cannot allocate device memory while they
+ * run: a real-time or latency-bound loop where an allocation (which can
+ * synchronise the whole device) is not allowed, or a plug-in whose host
+ * application owns the device memory budget through its own pool and
+ * forbids allocations behind its back.  The tile queue lives in a fixed
  * __device__ array inside the library (about 2.2 MB per device, held until
  * the process exits) instead of library-allocated memory, so the call never
- * calls cudaMalloc or cudaFree.  Limits: batch <= 4096 and
- * batch * ceil(max_dim/16)^2 <= 262144; larger calls return
- * BGEMM_ERROR_NOT_SUPPORTED.  d_info (device int, may be NULL) receives
- * bit 0 when a matrix size was negative or above max_dim (that matrix is
- * skipped); the caller clears it.  The first call on a device looks up the
- * array's address and should come before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race and must be ordered
- * by the caller. */
+ * calls cudaMalloc, cudaFree or any allocating routine.  Limits:
+ * batch <= 4096 and batch * ceil(max_dim/16)^2 <= 262144; larger calls
+ * return BGEMM_ERROR_NOT_SUPPORTED before any work is issued.  d_info
+ * (device int, may be NULL) receives bit 0 when a matrix size was negative
+ * or above max_dim (that matrix is skipped); the caller clears it.  With
+ * d_info == NULL such a matrix is skipped silently: nothing reports it.
+ * Set-up: the first call on a device looks up the array's device address
+ * and uploads the planner's small cost tables to that device (a
+ * synchronous copy); make that first call before any stream capture.
+ * All calls share the array and it keeps the last call's contents (each
+ * call clears the counters it needs): calls that overlap on the GPU race
+ * and must be ordered by the caller. */
 bgemm_status_t bgemm_framework_gemm_noalloc(const int* dM, const int* dN,
                                             const int* dK, float* const* dA,
                                             float* const* dB, float* const* dC,
                                             int batch, int max_dim, int* d_info,
                                             bgemm_stream_t stream);
+
+/* --- the one-shot entries' plan cache -------------------------------------
+ * No counterpart in the reference.  bgemm_plan_cache_set_limit sets the
+ * device bytes (per device) the cached plans of bgemm_sgemm_vbatched[_ex]
+ * may hold (0: the default, a third of the device's memory) and evicts down
+ * to it; bgemm_plan_cache_clear frees every evictable cached plan of the
+ * current device (waits for the device). */
+bgemm_status_t bgemm_plan_cache_set_limit(size_t bytes);
+bgemm_status_t bgemm_plan_cache_clear(void);
 
 /* --- errors and device facts --------------------------------------------- */
 /* 1-based position of the first invalid argument of the last failing call on

@@ -59,13 +59,21 @@ int bgemm_debug_framework_plan(const int* M, const int* N, const int* K, int bat
  * A hi, A lo, B hi, B lo byte offsets and kpad.  *n_jobs, *ws_used (bytes of
  * split operands), *ws_capacity (the scratch the entry sizes from its bounds)
  * and *err (the device error bits: 1 size out of bounds, 2 workspace too
- * small, 4 no costed configuration) are always written.  Returns the number
- * of work items, or -1 on invalid arguments or too small output arrays. */
+ * small, 4 no costed configuration) are always written; cfg_out[batch] (may
+ * be NULL) receives each matrix's CTA-pair configuration (-1: no tiles).
+ * Returns the number of work items, or -1 on invalid arguments or too small
+ * output arrays. */
 int bgemm_debug_framework_tc_plan(const int* M, const int* N, const int* K, int batch,
                                   int max_dim, int max_k, long long max_operand_elems, int mode,
                                   int* items_out, int max_items, int* jobs_out, int max_jobs,
                                   long long* ws_out, int* n_jobs, long long* ws_used,
-                                  long long* ws_capacity, int* err);
+                                  long long* ws_capacity, int* err, int* cfg_out);
+
+/* Cost-model entry of configuration `cfg` of `mode` (0 SIMT, 1 TF32,
+ * 2 TF32X3, 3 BF16X3): modelled time of one tile = *a_ns + *b_ns * K
+ * nanoseconds, as the device planners read it.  Returns 0, or -1 for an
+ * invalid mode or configuration. */
+int bgemm_debug_tile_cost(int mode, int cfg, float* a_ns, float* b_ns);
 
 /* Tensor-core plans: waits for `stream`, encodes on the host the tensor maps
  * that the device built for the plan, and compares them byte by byte.
@@ -85,6 +93,16 @@ int bgemm_debug_compare_tensor_maps(void* plan, void* stream, int* n_maps, int* 
  * if a CUDA call failed. */
 int bgemm_debug_bounded_wait_selftest(unsigned long long limit_ns, int* error, int* returned,
                                       int* wait_ok);
+
+/* Counters of the one-shot entries' plan cache on the current device:
+ * entries and device bytes held, and since the process started: calls that
+ * found their exact batch (hits), calls that re-planned a cached plan for
+ * the same shapes in another order (reorders), plans built (misses), plans
+ * freed to make room (evictions); *limit is the byte limit (0 until first
+ * set or used).  Every pointer may be NULL.  Returns 0. */
+int bgemm_debug_plan_cache_stats(long long* entries, long long* bytes, long long* hits,
+                                 long long* reorders, long long* misses, long long* evictions,
+                                 long long* limit);
 
 #ifdef __cplusplus
 }

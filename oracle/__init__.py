@@ -46,8 +46,17 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_ref_emul(ref_root: str = "/root/reference") -> Optional[str]:
+def reference_root() -> str:
+    """Where the BatchGEMM reference checkout is read from when the test
+    infrastructure builds from it: $BGEMM_REFERENCE_DIR, else the build
+    container's read-only checkout.  It is absent on machines that only run
+    the prebuilt files."""
+    return os.environ.get("BGEMM_REFERENCE_DIR", "/root/reference")
+
+
+def build_ref_emul(ref_root: Optional[str] = None) -> Optional[str]:
     """Build the reference-emulation binary (only where the reference exists)."""
+    ref_root = ref_root or reference_root()
     if not os.path.isdir(os.path.join(ref_root, "CUDA", "batching")):
         return None
     subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref_emul"), "REF=" + ref_root,
@@ -55,9 +64,10 @@ def build_ref_emul(ref_root: str = "/root/reference") -> Optional[str]:
     return os.path.join(REF_DIR, "ref_emul")
 
 
-def build_ref_gpu(ref_root: str = "/root/reference") -> Optional[str]:
+def build_ref_gpu(ref_root: Optional[str] = None) -> Optional[str]:
     """Build the reference framework kernels' cubin (only where the reference
     exists); returns its path, or the prebuilt one, or None."""
+    ref_root = ref_root or reference_root()
     out = os.path.join(REF_DIR, "ref_framework.cubin")
     if os.path.isdir(os.path.join(ref_root, "CUDA", "framework")):
         subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref_gpu"), "REF=" + ref_root,

@@ -2,7 +2,7 @@
 
 Run in a checkout that has the reference next to it:
 
-    python tests/golden/gen_golden.py [--ref /root/reference]
+    python tests/golden/gen_golden.py [--ref <reference checkout>]
 
 It writes
   * ``ref_kernels.npz`` -- seeded inputs and the outputs of the reference's own
@@ -52,7 +52,7 @@ CASES = [
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=oracle.reference_root())
     args = ap.parse_args()
     exe = oracle.build_ref_emul(args.ref)
     if exe is None:

@@ -26,7 +26,36 @@ import batchgemm_gb300 as bg
 MODES = {"tf32": 1, "tf32x3": 2, "bf16x3": 3}
 
 
-def fw_plan(M, N, K, max_dim, max_k, mode, elems=0):
+def quarter_octave(x):
+    """floor(4 log2 x) for x >= 1 from the float32 bits (the planners' bin
+    function, restated), 0 below 1."""
+    x = np.float32(x)
+    if not x >= 1:
+        return 0
+    u = int(np.array([x], np.float32).view(np.uint32)[0])
+    e = ((u >> 23) & 0xff) - 127
+    m = np.array([(u & 0x7fffff) | 0x3f800000], np.uint32).view(np.float32)[0]
+    edges = [np.float32(1.18920712), np.float32(1.41421356), np.float32(1.68179283)]
+    return 4 * e + sum(int(m >= q) for q in edges)
+
+
+def tile_bin(mode_id, cfg, K):
+    """Quarter-octave bin of the modelled tile time a + b*K (float32, as the
+    device computes it) of configuration cfg."""
+    L = bg.lib()
+    a, b = ctypes.c_float(), ctypes.c_float()
+    assert L.bgemm_debug_tile_cost(mode_id, cfg, ctypes.byref(a), ctypes.byref(b)) == 0
+    t = np.float32(a.value) + np.float32(b.value) * np.float32(K)
+    return min(63, max(0, quarter_octave(t) - 24))
+
+
+def assert_longest_first(items, cfgs, K, mode_id):
+    """Along the queue the modelled tile time's bin never increases."""
+    bins = [tile_bin(mode_id, cfgs[mat], K[mat]) for mat, _, _ in items]
+    assert all(b0 >= b1 for b0, b1 in zip(bins, bins[1:])), "queue not longest-first"
+
+
+def fw_plan(M, N, K, max_dim, max_k, mode, elems=0, with_cfg=False):
     L = bg.lib()
     n = len(M)
     ia = lambda v: (ctypes.c_int * max(n, 1))(*v)
@@ -36,11 +65,12 @@ def fw_plan(M, N, K, max_dim, max_k, mode, elems=0):
     f.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 3 + [ctypes.c_longlong, ctypes.c_int,
                                                               ctypes.c_void_p, ctypes.c_int,
                                                               ctypes.c_void_p, ctypes.c_int] + \
-        [ctypes.c_void_p] * 5
+        [ctypes.c_void_p] * 6
+    cfg = (ctypes.c_int * max(n, 1))()
     args = lambda items, mi, jobs, mj, ws: (ia(M), ia(N), ia(K), n, max_dim, max_k, elems,
                                             MODES[mode], items, mi, jobs, mj, ws,
                                             ctypes.byref(nj), ctypes.byref(used),
-                                            ctypes.byref(cap), ctypes.byref(err))
+                                            ctypes.byref(cap), ctypes.byref(err), cfg)
     cnt = f(*args(None, 0, None, 0, None))
     assert cnt >= 0
     items = (ctypes.c_int * max(3 * cnt, 1))()
@@ -48,8 +78,9 @@ def fw_plan(M, N, K, max_dim, max_k, mode, elems=0):
     ws = (ctypes.c_longlong * max(5 * n, 1))()
     cnt2 = f(*args(items, cnt, jobs, nj.value, ws))
     assert cnt2 == cnt
-    return (np.array(items[:3 * cnt]).reshape(-1, 3), np.array(jobs[:3 * nj.value]).reshape(-1, 3),
-            np.array(ws[:5 * n]).reshape(-1, 5), used.value, cap.value, err.value)
+    out = (np.array(items[:3 * cnt]).reshape(-1, 3), np.array(jobs[:3 * nj.value]).reshape(-1, 3),
+           np.array(ws[:5 * n]).reshape(-1, 5), used.value, cap.value, err.value)
+    return out + (list(cfg)[:n],) if with_cfg else out
 
 
 def batch(seed, n=80, max_dim=900, max_k=700):
@@ -100,7 +131,7 @@ def check_plan(M, N, K, mode, items, jobs, ws, used, cap, in_bounds):
         if not mats or mats[-1] != mat:
             assert mat not in mats
             mats.append(mat)
-    kbins = [min(63, int(4 * math.log2(K[m]))) for m in mats]
+    kbins = [min(63, quarter_octave(K[m])) for m in mats]
     assert kbins == sorted(kbins, reverse=True)
     # workspace panels: aligned, disjoint, inside the scratch
     esz = 2 if mode == "bf16x3" else 4
@@ -126,9 +157,11 @@ def test_device_planner_replay_covers_everything(built_lib, mode, seed):
     # the default bound (batch * 2 * max_dim * max_k) and the exact operand bound
     elems = sum((m + n) * k for m, n, k in zip(M, N, K))
     for bound in (0, elems):
-        items, jobs, ws, used, cap, err = fw_plan(M, N, K, 900, 700, mode, bound)
+        items, jobs, ws, used, cap, err, cfgs = fw_plan(M, N, K, 900, 700, mode, bound,
+                                                        with_cfg=True)
         assert err == 0
         check_plan(M, N, K, mode, items, jobs, ws, used, cap, [True] * len(M))
+        assert_longest_first(items, cfgs, K, MODES[mode])
 
 
 def test_device_planner_replay_flags_out_of_bounds(built_lib):
@@ -196,3 +229,15 @@ def test_simt_device_planner_replay(built_lib, seed):
             continue
         bm, bn = SIMT_CFGS[cfgs[i]]
         assert got == {(i, a, b) for a in range(-(-M[i] // bm)) for b in range(-(-N[i] // bn))}
+    assert_longest_first(items, cfgs, K, 0)
+
+
+def test_quarter_octave_bins_match_log2(built_lib):
+    """The integer bin function agrees with floor(4 log2 x) away from the
+    bin edges (where only the rounding of log2 could differ)."""
+    rng = np.random.default_rng(0)
+    for x in np.concatenate([np.exp(rng.uniform(0, 20, 2000)), np.arange(1, 3000)]):
+        x32 = np.float32(x)
+        v = 4 * math.log2(float(x32))
+        if abs(v - round(v)) > 1e-5:
+            assert quarter_octave(x32) == math.floor(v), x32

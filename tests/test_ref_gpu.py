@@ -144,3 +144,69 @@ def test_reference_kernel_timing(ref_kernel):
     t_ours = e[2].elapsed_time(e[3]) / reps
     print("\nreference gemm (strategy 2): %.3f ms = %.2f TFLOP/s; drop-in: %.3f ms = %.2f TFLOP/s"
           % (t_ref, flops / t_ref / 1e9, t_ours, flops / t_ours / 1e9))
+
+
+def _time(fn, reps=10, sync_each=False):
+    """Mean ms of `reps` calls after one warm-up, CUDA events on the current
+    stream; sync_each mirrors the reference's timed loop, which synchronises
+    the device after every launch (CUDA/framework/gemm.cu:203-214)."""
+    fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+        if sync_each:
+            torch.cuda.synchronize()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def test_reference_sweep_table(ref_kernel):
+    """Informational: the reference's published sweep (CUDA/framework/run.sh:
+    14-24, ./gemm B 512 6000 for B = 8 .. 256 over the first B rows of
+    data_MN_K_512_128; log-test-verify3:1-6) on this GPU.  GFLOP/s count
+    sum(2MNK + 2MN) as the reference does (gemm.cu:84-85), 10 launches each.
+
+    Columns: the reference kernel on strategy-2-compatible shapes (M, N of
+    the shape file rounded up to multiples of 32; its other tile bodies are
+    wrong as shipped and are not run), timed like the reference (device sync
+    after every launch) and back to back; the drop-in bgemm_framework_gemm
+    on the same arrays; the drop-in and the 3xTF32 mode on the shape file's
+    own sizes (C += A B)."""
+    from batchgemm_gb300 import workloads
+    rows = []
+    for B in (8, 16, 32, 64, 128, 256):
+        w = workloads.ref_dataset(B)
+        M32 = [(m + 31) // 32 * 32 for m in w.M]
+        N32 = [(n + 31) // 32 * 32 for n in w.N]
+        fl32 = sum(2.0 * m * n * k + 2.0 * m * n for m, n, k in zip(M32, N32, w.K))
+        bufs, ints = batch_arrays(M32, N32, w.K, B)
+        grid = (max(m // 32 for m in M32), max(n // 32 for n in N32), B)
+        args = (ints["M"].data_ptr(), ints["N"].data_ptr(), ints["K"].data_ptr(),
+                bufs["A"][1].data_ptr(), bufs["B"][1].data_ptr(), bufs["C"][1].data_ptr())
+        ref = lambda: ref_kernel.launch(grid, *args, ints["T"].data_ptr())
+        ours = lambda: bg.framework_gemm(*args, B, max(max(M32), max(N32)))
+        t_ref_sync = _time(ref, sync_each=True)
+        t_ref = _time(ref)
+        t_ours32 = _time(ours)
+        # the shape file's own sizes
+        fl = sum(2.0 * m * n * k + 2.0 * m * n for m, n, k in zip(w.M, w.N, w.K))
+        bufs2, ints2 = batch_arrays(w.M, w.N, w.K, B + 1)
+        args2 = (ints2["M"].data_ptr(), ints2["N"].data_ptr(), ints2["K"].data_ptr(),
+                 bufs2["A"][1].data_ptr(), bufs2["B"][1].data_ptr(), bufs2["C"][1].data_ptr())
+        t_ours = _time(lambda: bg.framework_gemm(*args2, B, max(max(w.M), max(w.N))))
+        ld = lambda v: bg.int_array([max(1, x) for x in v])
+        Mi, Ni, Ki = bg.int_array(w.M), bg.int_array(w.N), bg.int_array(w.K)
+        lda, ldb = ld(w.M), ld(w.K)
+        t_x3 = _time(lambda: bg.sgemm_vbatched(Mi, Ni, Ki, 1.0, args2[3], lda, args2[4], ldb,
+                                               1.0, args2[5], lda, mode="tf32x3"))
+        bg.framework_check_device()
+        rows.append((B, fl32 / t_ref_sync / 1e6, fl32 / t_ref / 1e6, fl32 / t_ours32 / 1e6,
+                     fl / t_ours / 1e6, fl / t_x3 / 1e6))
+    print("\nSWEEP | B | ref kernel s2, sync each | ref kernel s2 | drop-in (same) | "
+          "drop-in, file shapes | 3xTF32, file shapes |  (GFLOP/s, sum 2MNK + 2MN)")
+    for r in rows:
+        print("SWEEP | %d | %.1f | %.1f | %.1f | %.1f | %.1f |" % r)

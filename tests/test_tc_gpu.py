@@ -259,8 +259,8 @@ def test_skewed_full_size_error_vs_fp64(cuda, mode):
     torch.cuda.synchronize()
     smax, smean, _ = bench.fp64_sampled_error(db, per_matrix=4, seed=1)
     print("%s: max %.3g mean %.3g | simt max %.3g mean %.3g" % (mode, emax, emean, smax, smean))
-    if mode == "tf32x3":
-        assert emean <= 1.5 * smean
+    # the strict comparison with FP32 SIMT (mean and max) is
+    # test_error_bar_gpu.py::test_north_star_error_bar_skewed
 
 
 def test_bounded_wait_expires_and_context_survives(cuda):

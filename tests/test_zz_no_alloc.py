@@ -1,15 +1,14 @@
 """bgemm_framework_gemm_noalloc, the allocation-free variant of the device-queue
 FP32 entry point.
 
-Some callers cannot allocate device memory while they run: a stream that is
-being captured into a CUDA graph (an allocation is not capturable and breaks
-the capture), a real-time loop that must not risk the device-wide
-synchronisation an allocation can cause, a plug-in whose host application
-owns the memory budget.  For them the library keeps the tile queue in a fixed
-__device__ array instead of allocating it.  This file checks, through the C
-ABI, that two calls in a row give the same bits as the regular entry point
-(the FP32 SIMT tests' tolerance is bit-exactness), and that calls beyond the
-array's limits are refused before any work.  It is named to run last.
+Some callers cannot allocate device memory while they run: a real-time loop
+that must not risk the device-wide synchronisation an allocation can cause,
+or a plug-in whose host application owns the device memory budget through its
+own pool.  For them the library keeps the tile queue in a fixed __device__
+array instead of allocating it.  This file checks, through the C ABI, that two
+calls in a row give the same bits as the regular entry point (the FP32 SIMT
+tests' tolerance is bit-exactness), and that calls beyond the array's limits
+are refused before any work.  It is named to run last.
 """
 import ctypes
 
