@@ -297,7 +297,8 @@ bgemm_status_t tc_alloc(bgemm_plan_s* p) {
   p->info.kernels_per_execute = 2;
   if (t->pair) {
     // one CTA pair per cluster slot, never more pairs than tiles
-    const int pairs = std::max(1, std::min(t->clusters, std::max(p->cap.tiles, 1)));
+    int pairs = std::max(1, std::min(t->clusters, std::max(p->cap.tiles, 1)));
+    if (p->opt.max_ctas > 0) pairs = std::max(1, std::min(pairs, p->opt.max_ctas / 2));
     p->grid = 2 * pairs;
     p->info.grid = p->grid;
   }

@@ -166,7 +166,7 @@ struct Ring {
 
 // Bounded wait; returns false if the wait expired (error flag set) or
 // another role already aborted.
-__device__ __noinline__ bool wait_bounded(uint32_t bar, uint32_t parity, int* err,
+__device__ __forceinline__ bool wait_bounded(uint32_t bar, uint32_t parity, int* err,
                                           volatile int* abort, unsigned long long limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = gtimer();
@@ -185,7 +185,7 @@ __device__ __noinline__ bool wait_bounded(uint32_t bar, uint32_t parity, int* er
 
 // Bounded wait with cluster-scope acquire (barriers with arrivals from the
 // peer CTA or commits multicast by the leader).
-__device__ __noinline__ bool wait_bounded_cluster(uint32_t bar, uint32_t parity, int* err,
+__device__ __forceinline__ bool wait_bounded_cluster(uint32_t bar, uint32_t parity, int* err,
                                                   volatile int* abort,
                                                   unsigned long long limit_ns) {
   if (mbar_try_wait_cluster(bar, parity)) return true;
