@@ -51,7 +51,15 @@ struct Geo2 {
 constexpr int kSmemMax = Geo2<1>::SMEM > Geo2<0>::SMEM ? Geo2<1>::SMEM : Geo2<0>::SMEM;
 constexpr int kEpiWarps2 = 8;              // 2 per TMEM lane quadrant
 constexpr int kCols = 128;                 // accumulator columns per epilogue warp
-constexpr int kThreads2 = 64 + kEpiWarps2 * 32;
+// Three warpgroups: warpgroup 0 = producer (warp 0), MMA issuer (warp 1) and
+// two idle warps; warpgroups 1 and 2 = the 8 epilogue warps.  At launch every
+// thread gets 168 registers (3 warps per SM sub-partition); warpgroup 0 gives
+// most of its share to the epilogue warps, whose 128 accumulator columns per
+// lane would otherwise spill: 128 x 56 + 256 x 224 = 384 x 168.
+constexpr int kThreads2 = 384;
+constexpr int kEpiWarp0 = 4;               // first epilogue warp
+constexpr uint32_t kRegsCtl = 56, kRegsEpi = 224, kRegsLaunch = 168;
+static_assert(128 * kRegsCtl + 256 * kRegsEpi <= kThreads2 * kRegsLaunch, "register split");
 constexpr int kFineK2 = 64;
 // Matrices with K above kFineK2 promote every kGroupKB2 128-byte K slices.
 constexpr int kGroupKB2 = 2;
@@ -137,163 +145,171 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0) {
-    // ------------------------------------------------------------ producer
-    if (lane == 0) {
-      Ring st;
-      int inflight_phase[kS];
-      bool inflight[kS];
-      for (int s = 0; s < kS; ++s) inflight[s] = false, inflight_phase[s] = 0;
-      bool ok = true;
-      int last_mat = -1;
-      for (int t = 0; ok; ++t) {
-        const int it = snake(cl, t, ncl);
-        if (it >= n_items) break;
-        const TileItem ti = p.items[it];
-        const MatDesc d = p.descs[ti.mat];
-        const int bn = tc2_cfg_bn(d.cfg);
-        const int hb = bn >> 1;
-        const CUtensorMap* tm = p.tmaps + 4 * ti.mat;
-        if (ti.mat != last_mat && d.K > 0) {
-          for (int q = 0; q < 4; ++q) tmap_acquire(tm + q);
-          last_mat = ti.mat;
-        }
-        const int nk = (d.K + KE - 1) / KE;
-        const uint32_t tx = 2u * G::NP * (uint32_t)(kA + hb * 128);  // both CTAs, all parts
-        const int row_a = ti.tm * 256 + (int)rank * kRows;
-        const int row_b = ti.tn * bn + (int)rank * (tile_n(d, ti.tn, bn) >> 1);
-        for (int kb = 0; kb < nk; ++kb) {
-          if (!wait_bounded(empty(st.idx), st.phase ^ 1u, p.error, abort, p.timeout_ns)) {
-            ok = false;
-            break;
+  // Each warpgroup sets its register budget at one point that all four of
+  // its warps execute (setmaxnreg is warpgroup-aligned), ahead of the roles'
+  // code, so that the compiler allocates every role for its budget.
+  if (warp < kEpiWarp0) {
+    regs_shrink<kRegsCtl>();
+    if (warp == 0) {
+      // ------------------------------------------------------------ producer
+      if (lane == 0) {
+        Ring st;
+        // stages with a load in flight, and the phase each was loaded in (bit s)
+        uint32_t inflight = 0, inflight_phase = 0;
+        bool ok = true;
+        int last_mat = -1;
+        for (int t = 0; ok; ++t) {
+          const int it = snake(cl, t, ncl);
+          if (it >= n_items) break;
+          const TileItem ti = p.items[it];
+          const MatDesc d = p.descs[ti.mat];
+          const int bn = tc2_cfg_bn(d.cfg);
+          const int hb = bn >> 1;
+          const CUtensorMap* tm = p.tmaps + 4 * ti.mat;
+          if (ti.mat != last_mat && d.K > 0) {
+            for (int q = 0; q < 4; ++q) tmap_acquire(tm + q);
+            last_mat = ti.mat;
           }
-          const uint32_t sa = sbase + st.idx * kStage;
-          const uint32_t sb = sa + G::NP * kA;
-          const uint32_t fb = mapa_shared(full(st.idx), 0);
-          if (leader) {
-            mbar_arrive_expect_tx(full(st.idx), tx);
-            inflight[st.idx] = true;
-            inflight_phase[st.idx] = st.phase;
-          }
-          tma_load_2d_pair(sa, tm + 0, kb * KE, row_a, fb);
-          tma_load_2d_pair(sb, tm + 2, kb * KE, row_b, fb);
-          if (SPLIT) {
-            tma_load_2d_pair(sa + kA, tm + 1, kb * KE, row_a, fb);
-            tma_load_2d_pair(sb + kB, tm + 3, kb * KE, row_b, fb);
-          }
-          st.next(kS);
-        }
-      }
-      // The leader's full barriers count the bytes of both CTAs: once every
-      // phase it expected has completed, no copy of either CTA is in flight.
-      if (leader) {
-        for (int s = 0; s < kS; ++s)
-          if (inflight[s])
-            wait_bounded(full(s), (uint32_t)inflight_phase[s], p.error, nullptr, p.timeout_ns);
-      }
-      if (!ok) {
-        const uint64_t t0 = gtimer();  // aborted: give stray copies time to land
-        while (gtimer() - t0 < 200000ull) {
-        }
-      }
-    }
-    __syncwarp();
-  } else if (warp == 1) {
-    // -------------------------------------------------- MMA issue (leader)
-    if (lane == 0 && leader) {
-      Ring st, acc;
-      bool ok = true;
-      for (int t = 0; ok; ++t) {
-        const int it = snake(cl, t, ncl);
-        if (it >= n_items) break;
-        const TileItem ti = p.items[it];
-        const MatDesc d = p.descs[ti.mat];
-        const int bn = tc2_cfg_bn(d.cfg);
-        const uint32_t idesc = make_idesc_pair<KIND>(tile_n(d, ti.tn, bn));
-        const int nk = (d.K + KE - 1) / KE;
-        const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
-        const bool fine = SPLIT && d.K <= kFineK2;
-        for (int kb = 0; kb < nk; ++kb) {
-          if (!wait_bounded(full(st.idx), st.phase, p.error, abort, p.timeout_ns)) {
-            ok = false;
-            break;
-          }
-          tc_fence_after();
-          const uint32_t sa = sbase + st.idx * kStage;
-          const uint32_t sb = sa + G::NP * kA;
-          const int s_end = min(NSUB, nsub - kb * NSUB);
-          if (!SPLIT) {
-            // one product: a single accumulator per tile, the 2-deep ring
-            // alternating between tiles
-            if (kb == 0) {
-              if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
-                ok = false;
-                break;
-              }
-              tc_fence_after();
+          const int nk = (d.K + KE - 1) / KE;
+          const uint32_t tx = 2u * G::NP * (uint32_t)(kA + hb * 128);  // both CTAs, all parts
+          const int row_a = ti.tm * 256 + (int)rank * kRows;
+          const int row_b = ti.tn * bn + (int)rank * (tile_n(d, ti.tn, bn) >> 1);
+          for (int kb = 0; kb < nk; ++kb) {
+            if (!wait_bounded(empty(st.idx), st.phase ^ 1u, p.error, abort, p.timeout_ns)) {
+              ok = false;
+              break;
             }
-            const uint32_t buf = tmem + acc.idx * 256u;
-            for (int s = 0; s < s_end; ++s)
-              mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc,
-                             (kb > 0 || s > 0) ? 1u : 0u);
-            if (kb == nk - 1) {
-              mma_commit_pair(tfull(acc.idx));
-              acc.next(kNAcc);
+            const uint32_t sa = sbase + st.idx * kStage;
+            const uint32_t sb = sa + G::NP * kA;
+            const uint32_t fb = mapa_shared(full(st.idx), 0);
+            if (leader) {
+              mbar_arrive_expect_tx(full(st.idx), tx);
+              inflight |= 1u << st.idx;
+              inflight_phase = (inflight_phase & ~(1u << st.idx)) | (st.phase << st.idx);
             }
-          } else if (fine) {
-            for (int s = 0; s < s_end && ok; ++s) {
-              if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
-                ok = false;
-                break;
+            tma_load_2d_pair(sa, tm + 0, kb * KE, row_a, fb);
+            tma_load_2d_pair(sb, tm + 2, kb * KE, row_b, fb);
+            if (SPLIT) {
+              tma_load_2d_pair(sa + kA, tm + 1, kb * KE, row_a, fb);
+              tma_load_2d_pair(sb + kB, tm + 3, kb * KE, row_b, fb);
+            }
+            st.next(kS);
+          }
+        }
+        // The leader's full barriers count the bytes of both CTAs: once every
+        // phase it expected has completed, no copy of either CTA is in flight.
+        if (leader) {
+          for (int s = 0; s < kS; ++s)
+            if ((inflight >> s) & 1u)
+              wait_bounded(full(s), (inflight_phase >> s) & 1u, p.error, nullptr, p.timeout_ns);
+        }
+        if (!ok) {
+          const uint64_t t0 = gtimer();  // aborted: give stray copies time to land
+          while (gtimer() - t0 < 200000ull) {
+          }
+        }
+      }
+      __syncwarp();
+    } else if (warp == 1) {
+      // -------------------------------------------------- MMA issue (leader)
+      if (lane == 0 && leader) {
+        Ring st, acc;
+        bool ok = true;
+        for (int t = 0; ok; ++t) {
+          const int it = snake(cl, t, ncl);
+          if (it >= n_items) break;
+          const TileItem ti = p.items[it];
+          const MatDesc d = p.descs[ti.mat];
+          const int bn = tc2_cfg_bn(d.cfg);
+          const uint32_t idesc = make_idesc_pair<KIND>(tile_n(d, ti.tn, bn));
+          const int nk = (d.K + KE - 1) / KE;
+          const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
+          const bool fine = SPLIT && d.K <= kFineK2;
+          for (int kb = 0; kb < nk; ++kb) {
+            if (!wait_bounded(full(st.idx), st.phase, p.error, abort, p.timeout_ns)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sa = sbase + st.idx * kStage;
+            const uint32_t sb = sa + G::NP * kA;
+            const int s_end = min(NSUB, nsub - kb * NSUB);
+            if (!SPLIT) {
+              // one product: a single accumulator per tile, the 2-deep ring
+              // alternating between tiles
+              if (kb == 0) {
+                if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
+                  ok = false;
+                  break;
+                }
+                tc_fence_after();
               }
-              tc_fence_after();
               const uint32_t buf = tmem + acc.idx * 256u;
-              // small K: the split error dominates, so lo*lo is kept too
-              mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + kB + 32u * s),
-                             idesc, 0u);
-              mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
-              mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + kB + 32u * s), idesc, 1u);
-              mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
-              mma_commit_pair(tfull(acc.idx));
-              acc.next(kNAcc);
-            }
-            if (!ok) break;
-          } else {
-            // a group spans kGroupKB2 slices; small products of each slice first
-            const bool first = (kb % kGroupKB2) == 0;
-            if (first) {
-              if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
-                ok = false;
-                break;
+              for (int s = 0; s < s_end; ++s)
+                mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc,
+                               (kb > 0 || s > 0) ? 1u : 0u);
+              if (kb == nk - 1) {
+                mma_commit_pair(tfull(acc.idx));
+                acc.next(kNAcc);
               }
-              tc_fence_after();
+            } else if (fine) {
+              for (int s = 0; s < s_end && ok; ++s) {
+                if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
+                  ok = false;
+                  break;
+                }
+                tc_fence_after();
+                const uint32_t buf = tmem + acc.idx * 256u;
+                // small K: the split error dominates, so lo*lo is kept too
+                mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + kB + 32u * s),
+                               idesc, 0u);
+                mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + 32u * s), idesc,
+                               1u);
+                mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + kB + 32u * s), idesc,
+                               1u);
+                mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
+                mma_commit_pair(tfull(acc.idx));
+                acc.next(kNAcc);
+              }
+              if (!ok) break;
+            } else {
+              // a group spans kGroupKB2 slices; small products of each slice first
+              const bool first = (kb % kGroupKB2) == 0;
+              if (first) {
+                if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
+                  ok = false;
+                  break;
+                }
+                tc_fence_after();
+              }
+              const uint32_t buf = tmem + acc.idx * 256u;
+              for (int s = 0; s < s_end; ++s) {
+                mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + 32u * s), idesc,
+                               (first && s == 0) ? 0u : 1u);
+                mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + kB + 32u * s), idesc,
+                               1u);
+              }
+              for (int s = 0; s < s_end; ++s)
+                mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
+              if ((kb % kGroupKB2) == kGroupKB2 - 1 || kb == nk - 1) {
+                mma_commit_pair(tfull(acc.idx));
+                acc.next(kNAcc);
+              }
             }
-            const uint32_t buf = tmem + acc.idx * 256u;
-            for (int s = 0; s < s_end; ++s) {
-              mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + 32u * s), idesc,
-                             (first && s == 0) ? 0u : 1u);
-              mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + kB + 32u * s), idesc,
-                             1u);
-            }
-            for (int s = 0; s < s_end; ++s)
-              mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
-            if ((kb % kGroupKB2) == kGroupKB2 - 1 || kb == nk - 1) {
-              mma_commit_pair(tfull(acc.idx));
-              acc.next(kNAcc);
-            }
+            mma_commit_pair(empty(st.idx));
+            st.next(kS);
           }
-          mma_commit_pair(empty(st.idx));
-          st.next(kS);
         }
+        mma_commit_pair(drain);
+        wait_bounded(drain, 0, p.error, nullptr, p.timeout_ns);
       }
-      mma_commit_pair(drain);
-      wait_bounded(drain, 0, p.error, nullptr, p.timeout_ns);
-    }
-    __syncwarp();
+      __syncwarp();
+    }  // warps 2 and 3 are idle
   } else {
     // -------------------------------------------- epilogue (both CTAs)
-    const int q = warp & 3;
-    const int half = (warp - 2) >> 2;
+    regs_grow<kRegsEpi>();
+    const int q = warp & 3;  // TMEM lanes 32q .. 32q + 31
+    const int half = (warp - kEpiWarp0) >> 2;
     Ring acc;
     const float alpha = p.alpha, beta = p.beta;
     for (int t = 0;; ++t) {

@@ -164,6 +164,18 @@ struct Ring {
   }
 };
 
+// Per-warpgroup register budget (all four warps of the warpgroup execute
+// it).  The budgets of all warpgroups must add up to at most what the block
+// was launched with (threads x registers per thread at launch).
+template <uint32_t N>
+__device__ __forceinline__ void regs_shrink() {
+  asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(N));
+}
+template <uint32_t N>
+__device__ __forceinline__ void regs_grow() {
+  asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;\n" ::"n"(N));
+}
+
 // Bounded wait; returns false if the wait expired (error flag set) or
 // another role already aborted.
 __device__ __forceinline__ bool wait_bounded(uint32_t bar, uint32_t parity, int* err,
