@@ -84,9 +84,9 @@ KERNEL_FAMILIES = {"auto": 0, "single": 1, "pair": 2}
 class PlanOptions(ctypes.Structure):
     _fields_ = [("force_tile_config", ctypes.c_int), ("max_ctas", ctypes.c_int),
                 ("disable_rebalance", ctypes.c_int), ("host_tensor_maps", ctypes.c_int),
-                ("split_in_kernel", ctypes.c_int), ("kernel_family", ctypes.c_int),
+                ("kernel_family", ctypes.c_int),
                 ("layout", ctypes.c_int), ("trans_a", ctypes.c_int), ("trans_b", ctypes.c_int),
-                ("reserved", ctypes.c_int * 2), ("capacity", PlanRequirements)]
+                ("reserved", ctypes.c_int * 3), ("capacity", PlanRequirements)]
 
 
 LAYOUTS = {"col": 0, "row": 1}
@@ -103,7 +103,7 @@ def _op(v) -> int:
 
 
 def _options(force_tile_config=-1, max_ctas=0, rebalance=True, host_tensor_maps=False,
-             split_in_kernel=False, kernel_family="auto", capacity=None, layout="col",
+             kernel_family="auto", capacity=None, layout="col",
              trans_a=False, trans_b=False) -> PlanOptions:
     opt = PlanOptions()
     opt.layout = _layout(layout)
@@ -113,7 +113,6 @@ def _options(force_tile_config=-1, max_ctas=0, rebalance=True, host_tensor_maps=
     opt.max_ctas = max_ctas
     opt.disable_rebalance = 0 if rebalance else 1
     opt.host_tensor_maps = 1 if host_tensor_maps else 0
-    opt.split_in_kernel = 1 if split_in_kernel else 0
     opt.kernel_family = (KERNEL_FAMILIES[kernel_family] if isinstance(kernel_family, str)
                          else int(kernel_family))
     if capacity is not None:
@@ -154,6 +153,7 @@ def lib() -> ctypes.CDLL:
     L.bgemm_plan_capacity.argtypes = [vp, ctypes.POINTER(PlanRequirements)]
     L.bgemm_plan_check_device.argtypes = [vp, vp]
     L.bgemm_plan_set_kernel_events.argtypes = [vp, vp, vp]
+    L.bgemm_plan_set_cta_timer.argtypes = [vp, vp]
     L.bgemm_plan_destroy.argtypes = [vp]
     L.bgemm_framework_gemm.argtypes = [vp, vp, vp, vp, vp, vp, vp, i, i, vp]
     L.bgemm_framework_check_device.argtypes = [vp]
@@ -178,7 +178,8 @@ def lib() -> ctypes.CDLL:
                  "bgemm_plan_destroy", "bgemm_framework_gemm", "bgemm_framework_check_device",
                  "bgemm_framework_gemm_noalloc", "bgemm_framework_gemm_mode", "bgemm_framework_release",
                  "bgemm_device_info",
-                 "bgemm_plan_set_kernel_events", "bgemm_plan_requirements",
+                 "bgemm_plan_set_kernel_events", "bgemm_plan_set_cta_timer",
+                 "bgemm_plan_requirements",
                  "bgemm_plan_update", "bgemm_plan_capacity", "bgemm_sgemm_vbatched_ex",
                  "bgemm_plan_cache_set_limit", "bgemm_plan_cache_clear"):
         getattr(L, name).restype = i
@@ -261,13 +262,12 @@ class Plan:
 
     def __init__(self, M, N, K, lda, ldb, ldc, mode="simt", stream=None,
                  force_tile_config: int = -1, max_ctas: int = 0, rebalance: bool = True,
-                 host_tensor_maps: bool = False, split_in_kernel: bool = False,
-                 kernel_family="auto", capacity=None, layout="col", trans_a=False,
+                 host_tensor_maps: bool = False, kernel_family="auto", capacity=None, layout="col", trans_a=False,
                  trans_b=False):
         self._h = ctypes.c_void_p()
         self.batch = len(M)
         opt = _options(force_tile_config, max_ctas, rebalance, host_tensor_maps,
-                       split_in_kernel, kernel_family, capacity, layout, trans_a, trans_b)
+                       kernel_family, capacity, layout, trans_a, trans_b)
         _check(lib().bgemm_plan_create_ex(ctypes.byref(self._h), _iarr(M), _iarr(N), _iarr(K),
                                           _iarr(lda), _iarr(ldb), _iarr(ldc), len(M),
                                           _mode(mode), _stream(stream), ctypes.byref(opt)))
@@ -302,6 +302,11 @@ class Plan:
         the CUDA event exists)."""
         h = lambda e: None if e is None else (e.cuda_event or None)
         _check(lib().bgemm_plan_set_kernel_events(self._h, h(start), h(stop)))
+
+    def set_cta_timer(self, d_times=None) -> None:
+        """Per-CTA start/end global-timer stamps of the GEMM kernel into the
+        device buffer at address d_times (2 x grid uint64), or stop (None)."""
+        _check(lib().bgemm_plan_set_cta_timer(self._h, d_times))
 
     def close(self) -> None:
         if self._h:

@@ -974,6 +974,16 @@ bgemm_status_t bgemm_plan_capacity(bgemm_plan_t plan, bgemm_plan_requirements_t*
   return BGEMM_SUCCESS;
 }
 
+bgemm_status_t bgemm_plan_set_cta_timer(bgemm_plan_t plan, void* d_times) {
+  clear_error();
+  if (!plan) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
+  if (plan->mode == BGEMM_MODE_SIMT_FP32)
+    return set_error(BGEMM_ERROR_NOT_SUPPORTED, 1, -1,
+                     "per-CTA timing is a hook of the tensor-core GEMM kernels");
+  plan->d_cta_times = static_cast<unsigned long long*>(d_times);
+  return BGEMM_SUCCESS;
+}
+
 bgemm_status_t bgemm_plan_set_kernel_events(bgemm_plan_t plan, void* ev_start, void* ev_stop) {
   clear_error();
   if (!plan) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");

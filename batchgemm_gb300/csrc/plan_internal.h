@@ -80,6 +80,7 @@ struct bgemm_plan_s {
   bgemm::TcPlan* tc = nullptr;
   std::vector<bgemm::MatDesc> host_descs;
   bgemm_plan_info_t info{};
+  unsigned long long* d_cta_times = nullptr;  // profiling hook: per-CTA start/end times
   cudaEvent_t ev_start = nullptr;  // profiling hook around the GEMM launch
   cudaEvent_t ev_stop = nullptr;
 };

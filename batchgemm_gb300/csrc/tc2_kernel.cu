@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
   const bool leader = rank == 0;
   const int cl = blockIdx.x >> 1;
   const int ncl = gridDim.x >> 1;
+  if (p.cta_times && threadIdx.x == 0) p.cta_times[2 * blockIdx.x] = gtimer();
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kS; ++s) {
@@ -383,6 +384,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
   cluster_sync();
   tc_fence_after();
   if (warp == 1) tmem_dealloc_pair(tmem, 512);
+  if (p.cta_times && threadIdx.x == 0) p.cta_times[2 * blockIdx.x + 1] = gtimer();
 }
 
 template <int KIND, int SPLIT, bool BETA>

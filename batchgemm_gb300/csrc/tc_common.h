@@ -11,10 +11,7 @@
 namespace bgemm {
 
 // Element kinds of the packed operands.
-// kKindRaw: the pre-pass only transposes/compacts operands to K-major FP32
-// (4 B per element) and the GEMM splits them in shared memory (3xTF32 on
-// CTA pairs).
-enum TcKind : int { kKindTF32 = 0, kKindBF16 = 1, kKindRaw = 2 };
+enum TcKind : int { kKindTF32 = 0, kKindBF16 = 1 };
 
 // Tile configurations: UMMA M = 128 rows of the "A side" operand, UMMA N =
 // BN rows of the "B side".  Ids 0..3 keep A on the A side (BN 16/32/64/128);
@@ -71,6 +68,7 @@ struct TcGemmParams {
   float* const* C;
   int* error;                  // bit 0: a bounded device wait expired
   unsigned long long timeout_ns;
+  unsigned long long* cta_times;  // if set: [2 * blockIdx] start, [+1] end (global timer, ns)
 };
 
 // Device-side construction of the per-matrix tensor maps: one warp per map
@@ -108,8 +106,5 @@ int tc_smem_bytes(int kind, int split);
 cudaError_t tc2_gemm_launch(int kind, int split, const TcGemmParams& p, int grid,
                             cudaStream_t s);
 int tc2_max_clusters();
-// CTA-pair 3xTF32 kernel that splits raw FP32 operands in shared memory
-cudaError_t tc2s_gemm_launch(const TcGemmParams& p, int grid, cudaStream_t s);
-int tc2s_max_clusters();
 
 }  // namespace bgemm

@@ -75,9 +75,7 @@ constexpr int kEpiCols = kTcMaxBN / 2;
 // ---------------------------------------------------- operand splitting --
 __device__ __forceinline__ void put(char* hi, char* lo, long long idx, float x, int kind,
                                     int split) {
-  if (kind == kKindRaw) {
-    reinterpret_cast<float*>(hi)[idx] = x;
-  } else if (kind == kKindTF32) {
+  if (kind == kKindTF32) {
     const float h = round_keep(x, 13);
     reinterpret_cast<float*>(hi)[idx] = h;
     if (split) {
@@ -99,10 +97,6 @@ __device__ __forceinline__ void put(char* hi, char* lo, long long idx, float x, 
 // 16-byte (TF32) or 8-byte (BF16) store each; idx is a multiple of 4.
 __device__ __forceinline__ void put4(char* hi, char* lo, long long idx, const float* x, int kind,
                                      int split) {
-  if (kind == kKindRaw) {
-    *reinterpret_cast<float4*>(reinterpret_cast<float*>(hi) + idx) = make_float4(x[0], x[1], x[2], x[3]);
-    return;
-  }
   float h[4], l[4];
   const int drop = (kind == kKindTF32) ? 13 : 16;
 #pragma unroll
@@ -318,6 +312,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const int n_items = p.n_items_dev ? *p.n_items_dev : p.n_items;
+  if (p.cta_times && threadIdx.x == 0) p.cta_times[2 * blockIdx.x] = gtimer();
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
@@ -593,6 +588,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const TcGemmParams
   __syncthreads();
   tc_fence_after();
   if (warp == 1) tmem_dealloc(tmem, 512);
+  if (p.cta_times && threadIdx.x == 0) p.cta_times[2 * blockIdx.x + 1] = gtimer();
   if (threadIdx.x == 0) {
     __threadfence();
     const unsigned prev = atomicAdd(reinterpret_cast<unsigned*>(p.counters) + 1, 1u);

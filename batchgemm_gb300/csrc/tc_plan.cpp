@@ -20,9 +20,7 @@ struct TcPlan {
   int split = 1;             // the kernels read hi/lo pairs (kind TF32/BF16 split modes)
   bool split_mode = true;    // the plan's mode is TF32X3 or BF16X3
   int want_family = 0;       // 0: cost model, 1: one-SM, 2: CTA pair
-  bool raw_ok = false;       // TF32X3 with the in-kernel split requested
   bool pair = false;         // CTA-pair kernel (tc2_kernel.cu)
-  bool raw = false;          // 3xTF32 on pairs: raw FP32 operands split in the kernel
   int clusters = 0;          // CTA pairs resident at once
   bool host_tmaps = false;   // encode every tensor map on the host (comparison path)
   // capacity and device memory
@@ -80,7 +78,6 @@ bgemm_status_t tc_init(bgemm_plan_s* p, const bgemm_plan_options_t* opt, int clu
   t->split_mode = p->mode != BGEMM_MODE_TF32;
   t->split = t->split_mode ? 1 : 0;
   t->host_tmaps = opt->host_tensor_maps != 0;
-  t->raw_ok = p->mode == BGEMM_MODE_TF32X3 && opt->split_in_kernel;
   int fam = opt->kernel_family;
   if (fam < 0 || fam > 2)
     return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1, "kernel_family %d is not 0, 1 or 2", fam);
@@ -92,7 +89,7 @@ bgemm_status_t tc_init(bgemm_plan_s* p, const bgemm_plan_options_t* opt, int clu
                        opt->force_tile_config, forced, fam);
     fam = forced;
   }
-  t->clusters = clusters >= 0 ? clusters : t->raw_ok ? tc2s_max_clusters() : tc2_max_clusters();
+  t->clusters = clusters >= 0 ? clusters : tc2_max_clusters();
   if (fam == 2 && t->clusters < 1)
     return set_error(BGEMM_ERROR_NOT_SUPPORTED, 11, -1, "no CTA pair fits on this device");
   t->want_family = fam;
@@ -140,12 +137,6 @@ bgemm_status_t tc_choose(bgemm_plan_s* p, const int* M, const int* N, const int*
     g_pair = t->pair;
     st = choose_tiles(kTcNumCfgs, tc_eval, M, N, K, batch, t->pair ? t->clusters : single_slots,
                       opt, mp);
-  }
-  t->raw = t->pair && t->raw_ok;
-  if (t->raw) {
-    // 3xTF32 on CTA pairs: compact raw FP32 operands, split in the kernel
-    t->kind = kKindRaw;
-    t->split = 0;
   }
   return st;
 }
@@ -394,11 +385,11 @@ bgemm_status_t tc_execute(bgemm_plan_s* p, float alpha, const float* const* dA,
   cudaError_t e = tc_pack_launch(pp, t->pack_grid, stream);
   if (e != cudaSuccess) return cuda_error(e, "split/pack launch");
   TcGemmParams gp{p->d_descs, p->d_items, p->n_items, p->d_counters + kHdrItems,
-                  p->d_counters, t->d_tmaps, alpha, beta, dC, t->d_err, 2000000000ull};
+                  p->d_counters, t->d_tmaps, alpha, beta, dC, t->d_err, 2000000000ull,
+                  p->d_cta_times};
   if (p->ev_start) cudaEventRecord(p->ev_start, stream);
-  e = t->raw    ? tc2s_gemm_launch(gp, p->grid, stream)
-      : t->pair ? tc2_gemm_launch(t->kind, t->split, gp, p->grid, stream)
-                : tc_gemm_launch(t->kind, t->split, gp, p->grid, stream);
+  e = t->pair ? tc2_gemm_launch(t->kind, t->split, gp, p->grid, stream)
+              : tc_gemm_launch(t->kind, t->split, gp, p->grid, stream);
   if (p->ev_stop) cudaEventRecord(p->ev_stop, stream);
   if (e != cudaSuccess) return cuda_error(e, "tcgen05 GEMM launch");
   return BGEMM_SUCCESS;

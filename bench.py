@@ -367,6 +367,23 @@ def gpu_leg(args, rank, world, local):
     s.synchronize()
     plan.set_kernel_events(None, None)
     out["kernel_ms"] = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
+    if args.mode != "simt":
+        # load balance of the GEMM's static tile schedule: every persistent
+        # CTA stamps the global timer when it starts and when it finishes
+        stamps = torch.zeros(2 * info["grid"], dtype=torch.int64, device=dev)
+        plan.set_cta_timer(stamps.data_ptr())
+        with torch.cuda.stream(s):
+            db.execute(plan, w.alpha, w.beta, stream=s)
+        s.synchronize()
+        plan.set_cta_timer(None)
+        t = stamps.view(-1, 2).cpu().numpy().astype(np.float64)
+        span = t[:, 1].max() - t[:, 0].min()
+        out["cta_balance"] = {
+            "span_us": round(span / 1e3, 1),
+            "finish_spread_us": round((t[:, 1].max() - t[:, 1].min()) / 1e3, 1),
+            "mean_busy_frac": round(float((t[:, 1] - t[:, 0]).mean() / span), 4),
+            "how": "global-timer stamps of every persistent CTA at start and end of one GEMM "
+                   "launch (bgemm_plan_set_cta_timer)"}
     plan.close()
 
     # other modes on the same batch (a few steps each)
@@ -472,6 +489,8 @@ def gpu_leg(args, rank, world, local):
                            "pre_pass_traffic": pre_traffic}
         if mode != "bf16x3" and "bf16_tflops" in peaks:
             out["roofline"]["bf16_measured_tflops"] = peaks["bf16_tflops"]
+        if "cta_balance" in out:
+            out["roofline"]["cta_balance"] = out["cta_balance"]
 
     # end to end through the one-shot C-ABI call with host buffers.  Every
     # step copies its inputs in from pinned host memory, runs

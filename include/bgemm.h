@@ -114,18 +114,12 @@ typedef struct bgemm_plan_options {
   int disable_rebalance;    /* 1: skip the parallelism (wavefront) rebalance    */
   int host_tensor_maps;     /* 1: encode the TMA tensor maps on the host instead
                                of building them on the device (for comparison) */
-  int split_in_kernel;      /* 1: TF32X3 on CTA pairs loads raw FP32 operands (4 B
-                               per element) and splits them in shared memory
-                               instead of reading hi/lo pairs split by the
-                               pre-pass.  Fewer HBM/L2 bytes, but on GB300 the
-                               extra shared-memory traffic makes it slower, so
-                               it is off by default (kept for comparison). */
   int kernel_family;        /* split tensor-core modes: 0 chosen by the cost
                                model, 1 one-SM tiles, 2 CTA-pair tiles        */
   int layout;               /* bgemm_layout_t of every matrix (0: column-major) */
   int trans_a;              /* bgemm_op_t applied to every A (0: N)          */
   int trans_b;              /* bgemm_op_t applied to every B (0: N)          */
-  int reserved[2];
+  int reserved[3];          /* must be zero                                  */
   /* Capacity for bgemm_plan_update: each field is raised to the creating
    * batch's own requirement, so all-zero means "this batch only".
    * kernel_family is ignored here (see the field above). */
@@ -236,6 +230,14 @@ bgemm_status_t bgemm_plan_capacity(bgemm_plan_t plan,
  * Pass NULL, NULL to stop. */
 bgemm_status_t bgemm_plan_set_kernel_events(bgemm_plan_t plan, void* ev_start,
                                             void* ev_stop);
+/* Profiling hook of the tensor-core modes (no reference counterpart): every
+ * following bgemm_plan_execute makes each persistent CTA of the GEMM kernel
+ * write the device's global timer (ns) when it starts and when it finishes,
+ * to d_times[2*cta] and d_times[2*cta + 1] (a device array of 2 x
+ * bgemm_plan_info_t.grid unsigned 64-bit ints), so the spread of finish
+ * times -- the load imbalance of the static tile schedule -- can be read.
+ * Pass NULL to stop.  BGEMM_ERROR_NOT_SUPPORTED for FP32 SIMT plans. */
+bgemm_status_t bgemm_plan_set_cta_timer(bgemm_plan_t plan, void* d_times);
 /* Blocks until the plan's previous launches on `stream` finish and reports
  * BGEMM_ERROR_DEVICE_TIMEOUT if a device-side wait expired in any of them
  * (the flag is then cleared). */

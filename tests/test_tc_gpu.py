@@ -160,25 +160,6 @@ def test_every_tile_config(cuda, cfg):
     run_mode("tf32", M, N, K, 0.5, 0.0, force=cfg, seed=cfg)
 
 
-@pytest.mark.parametrize("cfg", [8, 9, 10, 12, 13, 14, -1])
-def test_split_in_kernel_variant(cuda, cfg):
-    """3xTF32 on CTA pairs with raw FP32 operands split in shared memory (opt-in)."""
-    rng = np.random.default_rng(cfg + 90)
-    M = rng.integers(1, 700, 12).tolist() + [1024]
-    N = rng.integers(1, 700, 12).tolist() + [1024]
-    K = rng.integers(0, 300, 12).tolist() + [1024]
-    db, host = make_batch(M, N, K, seed=cfg + 3)
-    with bg.Plan(db.M, db.N, db.K, db.lda, db.ldb, db.ldc, mode="tf32x3",
-                 force_tile_config=cfg if cfg >= 0 else 10, split_in_kernel=True) as p:
-        db.execute(p, 0.5, 0.25)
-        torch.cuda.synchronize()
-        p.check_device()
-    got = db.C.cpu().numpy()
-    guard_intact(db, host[2], got)
-    f64_check(db, host, got, 0.5, 0.25, 32.0, 2.0 ** -24)
-    split_check(db, host, got, 0.5, 0.25, oracle.MODE_TF32X3, 16.0)
-
-
 def test_pair_tiles_for_single_product(cuda):
     """The single-product TF32 mode runs on CTA pairs too (hi panels only,
     one accumulator per tile), including K = 0 and ragged edges."""
