@@ -263,6 +263,8 @@ bgemm_status_t fwtc_check_device(int dev) {
     if (err[0] || err[1]) {
       cudaMemset(kv.second.s.err, 0, sizeof(int));
       cudaMemset(kv.second.s.gemm_err, 0, sizeof(int));
+      // an aborted launch may have left the tile queue's counters mid-walk
+      if (err[1]) cudaMemset(kv.second.s.counters, 0, 2 * sizeof(int));
       if (err[1])
         return set_error(BGEMM_ERROR_DEVICE_TIMEOUT, 0, -1,
                          "a bounded wait in the tensor-core kernel expired; results are invalid");

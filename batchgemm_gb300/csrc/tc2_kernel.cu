@@ -15,16 +15,24 @@
 // TMEM buffer (2-deep ring) with the small products first, and the epilogue
 // warps of both CTAs add it into FP32 registers with round-to-nearest.
 //
-// Scheduling is static and needs no traffic between the CTAs: cluster c
-// takes queue items c, 2C-1-c, 2C+c, ... (a snake over the largest-first
-// queue, C clusters), so both CTAs of a pair walk the same tiles.
+// Scheduling is dynamic: the leader CTA's producer pulls the next item of
+// the largest-first queue with one atomic (fetched a tile ahead, so its
+// latency hides behind the current tile's loads) and publishes it in a
+// 4-slot ring in the shared memory of both CTAs (a remote store plus a
+// release.cluster arrive on the peer's barrier).  The leader's MMA lane, the
+// 16 epilogue warps of both CTAs and the peer's producer read each slot and
+// acknowledge it on the leader's sempty barrier; -1 ends the walk.  The last
+// cluster to finish resets the queue head, so graph replays need no memset.
 //
 // Synchronisation across the pair:
 //   full[s]   leader only: its producer expects the bytes of both CTAs; the
 //             peer's TMA completes on the leader's barrier (cta_group::2 TMA);
 //   empty[s]  both CTAs: the leader's commit is multicast to the pair;
 //   tfull[b]  both CTAs: multicast commit when a group's MMAs finish;
-//   tempty[b] leader only: 16 arrivals (8 epilogue warps x 2 CTAs).
+//   tempty[b] leader only: 16 arrivals (8 epilogue warps x 2 CTAs);
+//   sfull[j]  both CTAs: the leader's producer published schedule slot j;
+//   sempty[j] leader only: 18 arrivals (leader MMA lane, peer producer,
+//             8 epilogue warps x 2 CTAs) once slot j has been read.
 // All waits are bounded as in tc_kernel.cu.
 #include <stdint.h>
 
@@ -38,6 +46,7 @@ constexpr int kRows = 128;                 // A-side rows per CTA
 constexpr int kA = kRows * 128;            // 16 KB per part
 constexpr int kB = 128 * 128;              // B-side half: up to 128 rows
 constexpr int kNAcc = 2;                   // 256-column accumulator buffers
+constexpr int kSched = 4;                  // schedule slots (items published ahead)
 // Stage ring: split modes hold hi + lo of both sides (64 KB, 3 stages), the
 // single-product TF32 mode hi only (32 KB, 6 stages).
 template <int SPLIT>
@@ -45,8 +54,9 @@ struct Geo2 {
   static constexpr int NP = SPLIT ? 2 : 1;
   static constexpr int STAGE = NP * (kA + kB);
   static constexpr int S = SPLIT ? 3 : 6;
-  static constexpr int NBAR = 2 * S + 2 * kNAcc + 1;
-  static constexpr int SMEM = S * STAGE + NBAR * 8 + 16 + 1024;
+  static constexpr int NBAR = 2 * S + 2 * kNAcc + 1 + 2 * kSched;
+  // barriers | TMEM address, abort flag (16 B) | schedule slots | alignment
+  static constexpr int SMEM = S * STAGE + NBAR * 8 + 16 + 4 * kSched + 1024;
 };
 constexpr int kSmemMax = Geo2<1>::SMEM > Geo2<0>::SMEM ? Geo2<1>::SMEM : Geo2<0>::SMEM;
 constexpr int kEpiWarps2 = 8;              // 2 per TMEM lane quadrant
@@ -73,11 +83,6 @@ constexpr int kCPrefetchLead = 2;
 __device__ __forceinline__ int tile_n(const MatDesc& d, int tn, int bn) {
   const int rem = (tc_cfg_swap(d.cfg) ? d.M : d.N) - tn * bn;
   return min(bn, (rem + 15) & ~15);
-}
-
-__device__ __forceinline__ int snake(int c, int t, int ncl) {
-  const int base = t * ncl;
-  return (t & 1) ? base + (ncl - 1 - c) : base + c;
 }
 
 template <int KIND>
@@ -109,16 +114,19 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
   auto tfull = [&](int s) { return bar0 + 8u * (2 * kS + s); };
   auto tempty = [&](int s) { return bar0 + 8u * (2 * kS + kNAcc + s); };
   const uint32_t drain = bar0 + 8u * (2 * kS + 2 * kNAcc);
+  auto sfull = [&](int j) { return bar0 + 8u * (2 * kS + 2 * kNAcc + 1 + j); };
+  auto sempty = [&](int j) { return bar0 + 8u * (2 * kS + 2 * kNAcc + 1 + kSched + j); };
   volatile uint32_t* tmem_slot =
       reinterpret_cast<volatile uint32_t*>(smem + kS * kStage + kNBar * 8);
   volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  volatile int* slots = reinterpret_cast<volatile int*>(tmem_slot + 4);
+  const uint32_t slots_addr = smem_u32(const_cast<int*>(slots));
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const int n_items = p.n_items_dev ? *p.n_items_dev : p.n_items;
   const uint32_t rank = cluster_ctarank();
   const bool leader = rank == 0;
-  const int cl = blockIdx.x >> 1;
   const int ncl = gridDim.x >> 1;
   if (p.cta_times && threadIdx.x == 0) p.cta_times[2 * blockIdx.x] = gtimer();
 
@@ -130,6 +138,10 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
     for (int s = 0; s < kNAcc; ++s) {
       mbar_init(tfull(s), 1);
       mbar_init(tempty(s), 2 * kEpiWarps2);
+    }
+    for (int j = 0; j < kSched; ++j) {
+      mbar_init(sfull(j), 1);
+      mbar_init(sempty(j), 2 + 2 * kEpiWarps2);
     }
     mbar_init(drain, 1);
     *abort = 0;
@@ -154,14 +166,55 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
     if (warp == 0) {
       // ------------------------------------------------------------ producer
       if (lane == 0) {
-        Ring st;
+        Ring st, sc;
         // stages with a load in flight, and the phase each was loaded in (bit s)
         uint32_t inflight = 0, inflight_phase = 0;
         bool ok = true;
         int last_mat = -1;
-        for (int t = 0; ok; ++t) {
-          const int it = snake(cl, t, ncl);
-          if (it >= n_items) break;
+        // The leader publishes each item one tile ahead of its own loads, so
+        // the peer's producer and the consumers find the next item ready.
+        auto pull = [&]() {
+          const int v = atomicAdd(p.counters, 1);
+          return v < n_items ? v : -1;
+        };
+        auto publish = [&](int v) {
+          if (!wait_bounded_cluster(sempty(sc.idx), sc.phase ^ 1u, p.error, abort, p.timeout_ns))
+            return false;
+          slots[sc.idx] = v;
+          st_cluster_u32(mapa_shared(slots_addr + 4u * sc.idx, 1), (uint32_t)v);
+          mbar_arrive(sfull(sc.idx));
+          mbar_arrive_cluster(mapa_shared(sfull(sc.idx), 1));
+          sc.next(kSched);
+          return true;
+        };
+        int cur = -1, nxt = -1;
+        if (leader) {
+          cur = pull();
+          ok = publish(cur);
+          if (ok && cur >= 0) nxt = pull();
+        }
+        while (ok) {
+          int it;
+          if (leader) {
+            it = cur;
+            if (it < 0) break;
+            if (!publish(nxt)) {
+              ok = false;
+              break;
+            }
+            const int after = nxt >= 0 ? pull() : -1;
+            cur = nxt;
+            nxt = after;
+          } else {
+            if (!wait_bounded_cluster(sfull(sc.idx), sc.phase, p.error, abort, p.timeout_ns)) {
+              ok = false;
+              break;
+            }
+            it = slots[sc.idx];
+            mbar_arrive_cluster(mapa_shared(sempty(sc.idx), 0));
+            sc.next(kSched);
+            if (it < 0) break;
+          }
           const TileItem ti = p.items[it];
           const MatDesc d = p.descs[ti.mat];
           const int bn = tc2_cfg_bn(d.cfg);
@@ -196,6 +249,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
             }
             st.next(kS);
           }
+          if (!ok) break;
         }
         // The leader's full barriers count the bytes of both CTAs: once every
         // phase it expected has completed, no copy of either CTA is in flight.
@@ -214,11 +268,14 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
     } else if (warp == 1) {
       // -------------------------------------------------- MMA issue (leader)
       if (lane == 0 && leader) {
-        Ring st, acc;
+        Ring st, acc, sc;
         bool ok = true;
-        for (int t = 0; ok; ++t) {
-          const int it = snake(cl, t, ncl);
-          if (it >= n_items) break;
+        while (ok) {
+          if (!wait_bounded(sfull(sc.idx), sc.phase, p.error, abort, p.timeout_ns)) break;
+          const int it = slots[sc.idx];
+          mbar_arrive(sempty(sc.idx));
+          sc.next(kSched);
+          if (it < 0) break;
           const TileItem ti = p.items[it];
           const MatDesc d = p.descs[ti.mat];
           const int bn = tc2_cfg_bn(d.cfg);
@@ -311,11 +368,30 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
     regs_grow<kRegsEpi>();
     const int q = warp & 3;  // TMEM lanes 32q .. 32q + 31
     const int half = (warp - kEpiWarp0) >> 2;
-    Ring acc;
+    Ring acc, sc;
     const float alpha = p.alpha, beta = p.beta;
-    for (int t = 0;; ++t) {
-      const int it = snake(cl, t, ncl);
-      if (it >= n_items) break;
+    // Reads the next schedule slot (lane 0) and acknowledges it to the
+    // leader.  The acknowledgment is a cluster-scope release, which waits for
+    // this lane's earlier global stores; so the next item is fetched before a
+    // tile's C stores, never right after them.
+    auto fetch = [&]() {
+      int v = -1;
+      if (lane == 0) {
+        // the peer's slots are written by the leader's producer (release.cluster)
+        const bool got = leader ? wait_bounded(sfull(sc.idx), sc.phase, p.error, abort,
+                                               p.timeout_ns)
+                                : wait_bounded_cluster(sfull(sc.idx), sc.phase, p.error, abort,
+                                                       p.timeout_ns);
+        if (got) {
+          v = slots[sc.idx];
+          mbar_arrive_cluster(mapa_shared(sempty(sc.idx), 0));
+        }
+      }
+      sc.next(kSched);
+      return __shfl_sync(0xffffffffu, v, 0);
+    };
+    int it = fetch();
+    while (it >= 0) {
       const TileItem ti = p.items[it];
       const MatDesc d = p.descs[ti.mat];
       float* C = p.C[ti.mat];
@@ -372,6 +448,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
         acc.next(kNAcc);
       }
       if (!ok) break;
+      it = fetch();
       if constexpr (BETA)
         c_store<kCols, 16>(r, C, ldc, d.M, d.N, swap, row0, col_base, ncols, alpha, beta, lane);
       else
@@ -384,6 +461,17 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
   cluster_sync();
   tc_fence_after();
   if (warp == 1) tmem_dealloc_pair(tmem, 512);
+  if (leader && threadIdx.x == 0) {
+    // the last cluster to finish resets the queue for the next launch (every
+    // leader has pulled its final item before it gets here)
+    __threadfence();
+    const unsigned prev = atomicAdd(reinterpret_cast<unsigned*>(p.counters) + 1, 1u);
+    if (prev == (unsigned)ncl - 1) {
+      atomicExch(p.counters, 0);
+      atomicExch(p.counters + 1, 0);
+      __threadfence();
+    }
+  }
   if (p.cta_times && threadIdx.x == 0) p.cta_times[2 * blockIdx.x + 1] = gtimer();
 }
 

@@ -402,6 +402,8 @@ bgemm_status_t tc_check_device(bgemm_plan_s* p, cudaStream_t) {
   if (e != cudaSuccess) return cuda_error(e, "device error word");
   if (err) {
     cudaMemset(t->d_err, 0, sizeof(int));
+    // an aborted launch may have left the tile queue's counters mid-walk
+    cudaMemset(p->d_counters, 0, 2 * sizeof(int));
     return set_error(BGEMM_ERROR_DEVICE_TIMEOUT, 0, -1,
                      "a bounded wait in the tensor-core kernel expired; results are invalid");
   }
