@@ -173,6 +173,9 @@ def lib() -> ctypes.CDLL:
     ll = ctypes.POINTER(ctypes.c_longlong)
     L.bgemm_debug_plan_cache_stats.argtypes = [ll] * 7
     L.bgemm_debug_plan_cache_stats.restype = i
+    L.bgemm_debug_set_tc_schedule.argtypes = [i, vp]
+    L.bgemm_debug_get_tc_schedule.argtypes = [i, vp]
+    L.bgemm_debug_tile_cost.argtypes = [i, i, ctypes.POINTER(f), ctypes.POINTER(f)]
     for name in ("bgemm_sgemm_vbatched", "bgemm_plan_create", "bgemm_plan_create_ex",
                  "bgemm_plan_execute", "bgemm_plan_info", "bgemm_plan_check_device",
                  "bgemm_plan_destroy", "bgemm_framework_gemm", "bgemm_framework_check_device",

@@ -1,14 +1,31 @@
-"""Autotuner of the planners' tile cost table.
+"""Autotuner of the planners' tile cost table and of the tensor-core
+promotion schedule.
 
-For every mode and every tile configuration it runs uniform batches whose
-matrices are whole multiples of the tile (several waves of persistent CTAs),
-at several K, with the configuration forced and the rebalance off; the time
-of one tile, t = a + b*K, is fitted by least squares and written to
-``csrc/tile_table_tuned.inc``, which the library compiles in place of the
-analytic defaults of ``csrc/tile_table.h``.
+Tile costs.  For every mode and every tile configuration it runs uniform
+batches whose matrices are whole multiples of the tile (several waves of
+persistent CTAs), at several K, with the configuration forced and the
+rebalance off; the time of one tile, t = a + b*K, is fitted by least squares.
 
-  python -m batchgemm_gb300.autotune            # measure and print
-  python -m batchgemm_gb300.autotune --write    # ... and write the table
+Promotion schedule (--schedule).  The split modes on CTA pairs accumulate a
+group of 128-byte K slices in tensor memory before the epilogue promotes the
+group into FP32 registers; longer groups drain tensor memory less often
+(faster) but let the tensor core's truncating accumulation run longer (less
+accurate).  For each bucket of K (K <= 64, then one octave per bucket) and
+each candidate group length (0 = promote every MMA and keep lo*lo) it times
+the GEMM kernel on 24 matrices of 1024 x 1024 x K (N(0, 1) entries) and
+measures the normalised error against FP64 on fixed samples, next to the FP32
+SIMT path's error on the same samples.  It keeps the fastest group whose mean
+and maximum error are both no worse than FP32 SIMT's (3xBF16, whose split
+error is far above FP32's: the fastest within 2 % of its most accurate
+group's mean).
+
+Both results are written to ``csrc/tile_table_tuned.inc``, which the library
+compiles in place of the analytic defaults of ``csrc/tile_table.h``; what a
+run does not measure is copied from the library's current tables.
+
+  python -m batchgemm_gb300.autotune                     # tile costs, print
+  python -m batchgemm_gb300.autotune --write             # ... and write
+  python -m batchgemm_gb300.autotune --schedule --write  # schedule, write
 
 The split/pack pre-pass of the tensor-core modes does not depend on the tile
 configuration; its time is estimated from its bytes (read 4 B, write 4 or 8
@@ -96,17 +113,167 @@ def fit(Ks, ts):
     return max(a, 50.0), max(b, 1e-3)
 
 
+SCHED_BUCKET_K = [48, 96, 192, 384, 768, 1536, 3072, 6144]  # one K per bucket
+SCHED_CANDIDATES = [0, 1, 2, 3, 4, 6, 8]
+
+
+def sched_measure(mode, K, group, n=24, size=1024, reps=5, samples=128):
+    """GEMM-kernel time (ms, best of reps) and sampled errors (numpy) of one
+    promotion group length on n matrices of size x size x K."""
+    import ctypes
+    import torch
+    import batchgemm_gb300 as bg
+    from batchgemm_gb300.accuracy import fp64_sampled_error
+    from batchgemm_gb300.batch import DeviceBatch
+    L = bg.lib()
+    mid = MODE_IDS[mode]
+    prev = (ctypes.c_int * 8)()
+    L.bgemm_debug_get_tc_schedule(mid, prev)
+    g = list(prev)
+    g[_bucket(K)] = group
+    assert L.bgemm_debug_set_tc_schedule(mid, (ctypes.c_int * 8)(*g)) == 0
+    try:
+        db = DeviceBatch([size] * n, [size] * n, [K] * n).fill_fast("normal", 0)
+        best = float("inf")
+        with db.plan(mode, kernel_family="pair") as p:
+            for _ in range(2):
+                db.execute(p, 1.0, 0.0)
+            torch.cuda.synchronize()
+            for _ in range(reps):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                e1.record()
+                p.set_kernel_events(e0, e1)
+                db.execute(p, 1.0, 0.0)
+                e1.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            p.set_kernel_events(None, None)
+            p.check_device()
+        err, _ = fp64_sampled_error(db, per_matrix=samples, seed=7, samples=True)
+        db.C.zero_()
+        with db.plan("simt") as ps:
+            db.execute(ps, 1.0, 0.0)
+        torch.cuda.synchronize()
+        serr, _ = fp64_sampled_error(db, per_matrix=samples, seed=7, samples=True)
+        del db
+        torch.cuda.empty_cache()
+        return best, err, serr
+    finally:
+        L.bgemm_debug_set_tc_schedule(mid, (ctypes.c_int * 8)(*list(prev)))
+
+
+def _bucket(K):
+    if K <= 64:
+        return 0
+    b, v = 0, (K - 1) >> 6
+    while v > 1:
+        v >>= 1
+        b += 1
+    return min(b + 1, 7)
+
+
+def sweep_schedule(modes):
+    """Per mode and bucket of K: the fastest group length within the error bar."""
+    out = {}
+    for mode in modes:
+        row = []
+        for b, K in enumerate(SCHED_BUCKET_K):
+            nk = -(-K // (32 if mode != "bf16x3" else 64))  # 128-byte slices
+            cands = [g for g in SCHED_CANDIDATES if g == 0 or g <= max(nk, 1)]
+            if b > 0:
+                cands = [g for g in cands if g != 0 or K <= 128]
+            res = []
+            for g in cands:
+                ms, e, se = sched_measure(mode, K, g)
+                res.append((g, ms, float(e.mean()), float(e.max()), float(se.mean()),
+                            float(se.max())))
+                print("schedule %-6s K=%-5d group %d  %.4f ms  err mean %.3g max %.3g  |  "
+                      "simt mean %.3g max %.3g" % ((mode, K) + res[-1]), flush=True)
+            if mode == "tf32x3":
+                ok = [r for r in res if r[2] <= r[4] and r[3] <= r[5]]
+            else:
+                best_mean = min(r[2] for r in res)
+                ok = [r for r in res if r[2] <= 1.02 * best_mean]
+            pick = min(ok, key=lambda r: r[1]) if ok else min(res, key=lambda r: r[2])
+            print("schedule %-6s K=%-5d -> group %d" % (mode, K, pick[0]), flush=True)
+            row.append(pick[0])
+        out[mode] = row
+    return out
+
+
+def current_tables():
+    """The library's compiled cost tables and schedule (to fill in what a run
+    does not measure)."""
+    import ctypes
+    import batchgemm_gb300 as bg
+    L = bg.lib()
+    a, b = ctypes.c_float(), ctypes.c_float()
+    simt = []
+    for c in range(8):
+        L.bgemm_debug_tile_cost(0, c, ctypes.byref(a), ctypes.byref(b))
+        simt.append((a.value, b.value))
+    tc = {}
+    for mode, mid in MODE_IDS.items():
+        row = []
+        for c in range(16):
+            L.bgemm_debug_tile_cost(mid, c, ctypes.byref(a), ctypes.byref(b))
+            row.append((a.value, b.value) if b.value > 0 else None)
+        tc[mode] = row
+    sched = {}
+    for mode, mid in MODE_IDS.items():
+        g = (ctypes.c_int * 8)()
+        L.bgemm_debug_get_tc_schedule(mid, g)
+        sched[mode] = list(g)
+    return simt, tc, sched
+
+
+def write_table(out, simt, tc, sched, dev_name, num_sms):
+    def row(v):
+        return "{%.1ff, %.4ff}" % tuple(v) if v else "{0.f, 0.f}"
+    lines = [
+        "// Generated by batchgemm_gb300/autotune.py on %s (%s, %d SMs); do not edit." % (
+            datetime.date.today().isoformat(), dev_name, num_sms),
+        "// Per-tile time t = a + b*K in ns, measured with every persistent CTA busy.",
+        "constexpr TileCost kSimtCost[8] = {%s};" % ", ".join(row(v) for v in simt),
+        "constexpr TileCost kTcCost[3][16] = {\n%s};" % ",\n".join(
+            "  {%s}" % ", ".join(row(v) for v in tc[m]) for m in ("tf32", "tf32x3", "bf16x3")),
+        "// Promotion groups of the split modes on CTA pairs per bucket of K (128-byte",
+        "// K slices; 0 = every MMA, lo*lo kept): the fastest within the error bar.",
+        "#define BGEMM_TUNED_HAS_SCHEDULE 1",
+        "constexpr unsigned char kTcGroupTable[3][8] = {%s};" % ", ".join(
+            "{%s}" % ", ".join(str(int(x)) for x in sched[m]) for m in ("tf32", "tf32x3",
+                                                                        "bf16x3")),
+    ]
+    with open(out, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    print("wrote", out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--write", action="store_true")
     ap.add_argument("--out", default=os.path.join(PKG, "csrc", "tile_table_tuned.inc"))
     ap.add_argument("--modes", default="simt,tf32,tf32x3,bf16x3")
+    ap.add_argument("--schedule", action="store_true",
+                    help="sweep the promotion schedule instead of the tile costs")
     ap.add_argument("--json", default=None, help="also dump raw measurements here")
     args = ap.parse_args()
     import torch
     import batchgemm_gb300 as bg
     bg.lib()
     dev = bg.device_info()
+    simt_cur, tc_cur, sched_cur = current_tables()
+    if args.schedule:
+        modes = [m for m in args.modes.split(",") if m in ("tf32x3", "bf16x3")]
+        sched = dict(sched_cur)
+        sched.update(sweep_schedule(modes))
+        if args.json:
+            json.dump(sched, open(args.json, "w"), indent=1)
+        if args.write:
+            write_table(args.out, simt_cur, tc_cur, sched, torch.cuda.get_device_name(0),
+                        dev["num_sms"])
+        return
     peaks = {}
     pk = os.path.join(os.path.dirname(PKG), "MEASURED_PEAKS.json")
     if os.path.exists(pk):
@@ -115,8 +282,8 @@ def main():
     simt_slots = dev["num_sms"] * dev["simt_ctas_per_sm"]
     tc_slots = dev["num_sms"] * dev["tc_ctas_per_sm"]
     raw = {}
-    simt = [None] * 8
-    tc = {m: [None] * 16 for m in MODE_IDS}
+    simt = list(simt_cur)
+    tc = {m: list(v) for m, v in tc_cur.items()}
     for mode in args.modes.split(","):
         Ks = [16, 64, 256, 1024] if mode == "simt" else [32, 128, 512, 2048]
         cfgs = range(8) if mode == "simt" else [c for c in range(16) if valid_tc(mode, c)]
@@ -136,29 +303,9 @@ def main():
                 tc[mode][c] = (a, b)
     if args.json:
         json.dump(raw, open(args.json, "w"), indent=1)
-    if not args.write:
-        return
-    # keep analytic defaults for anything not measured in this run
-    lines = [
-        "// Generated by batchgemm_gb300/autotune.py on %s (%s, %d SMs); do not edit." % (
-            datetime.date.today().isoformat(), torch.cuda.get_device_name(0), dev["num_sms"]),
-        "// Per-tile time t = a + b*K in ns, measured with every persistent CTA busy.",
-    ]
-    def row(v):
-        return "{%.1ff, %.4ff}" % v if v else "{0.f, 0.f}"
-    if any(v is None for v in simt):
-        sys.exit("the SIMT table needs every configuration measured (run with simt in --modes)")
-    lines.append("constexpr TileCost kSimtCost[8] = {%s};" % ", ".join(row(v) for v in simt))
-    rows = []
-    for mode in ("tf32", "tf32x3", "bf16x3"):
-        if all(v is None for v in tc[mode]):
-            sys.exit("mode %s was not measured" % mode)
-        rows.append("  {%s}" % ", ".join(row(v) for v in tc[mode]))
-    lines.append("constexpr TileCost kTcCost[3][16] = {\n%s};" % ",\n".join(rows))
-    out = args.out
-    with open(out, "w") as f:
-        f.write("\n".join(lines) + "\n")
-    print("wrote", out)
+    if args.write:
+        write_table(args.out, simt, tc, sched_cur, torch.cuda.get_device_name(0),
+                    dev["num_sms"])
 
 
 if __name__ == "__main__":

@@ -418,7 +418,7 @@ extern "C" bgemm_status_t bgemm_framework_gemm_mode(const int* dM, const int* dN
   e = tc_pack_launch(pp, df.num_sms * 8, stream);
   if (e != cudaSuccess) return cuda_error(e, "split/pack launch");
   TcGemmParams gp{s.descs, s.items, 0, s.counts, s.counters, s.tmaps, 1.0f, 1.0f, dC,
-                  s.gemm_err, 2000000000ull};
+                  s.gemm_err, 2000000000ull, nullptr, tc_schedule(mode)};
   e = tc2_gemm_launch(kind, split, gp, 2 * clusters, stream);
   if (e != cudaSuccess) return cuda_error(e, "tcgen05 GEMM launch");
   return BGEMM_SUCCESS;

@@ -10,10 +10,12 @@
 // the L2 traffic per flop of the one-SM kernel (tc_kernel.cu), which is what
 // bounds that kernel.
 //
-// Accumulation is group-promoted exactly as in tc_kernel.cu: each group (two
-// 128-byte K slices, or one MMA for K <= 64) accumulates into a fresh 256-column
-// TMEM buffer (2-deep ring) with the small products first, and the epilogue
-// warps of both CTAs add it into FP32 registers with round-to-nearest.
+// Accumulation is group-promoted as in tc_kernel.cu: each group accumulates
+// into a fresh 256-column TMEM buffer (2-deep ring) with the small products
+// first, and the epilogue warps of both CTAs add it into FP32 registers with
+// round-to-nearest.  The group length per bucket of K comes from the launch's
+// autotuned TcSchedule (a number of 128-byte K slices, or one MMA with lo*lo
+// kept on the small-K path).
 //
 // Scheduling is dynamic: the leader CTA's producer pulls the next item of
 // the largest-first queue with one atomic (fetched a tile ahead, so its
@@ -70,9 +72,12 @@ constexpr int kThreads2 = 384;
 constexpr int kEpiWarp0 = 4;               // first epilogue warp
 constexpr uint32_t kRegsCtl = 56, kRegsEpi = 224, kRegsLaunch = 168;
 static_assert(128 * kRegsCtl + 256 * kRegsEpi <= kThreads2 * kRegsLaunch, "register split");
-constexpr int kFineK2 = 64;
-// Matrices with K above kFineK2 promote every kGroupKB2 128-byte K slices.
-constexpr int kGroupKB2 = 2;
+// Promotion groups of the split modes come per bucket of K from the launch's
+// TcSchedule (autotuned table): group g > 0 = g 128-byte K slices per TMEM
+// buffer, g = 0 = the small-K path (promote every MMA, keep lo*lo).
+__device__ __forceinline__ int group_slices(const TcGemmParams& p, int K) {
+  return p.sched.group(tc_sched_bucket(K));
+}
 // beta != 0: promotion groups before the tile's end at which C is prefetched
 constexpr int kCPrefetchLead = 2;
 
@@ -282,7 +287,9 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
           const uint32_t idesc = make_idesc_pair<KIND>(tile_n(d, ti.tn, bn));
           const int nk = (d.K + KE - 1) / KE;
           const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
-          const bool fine = SPLIT && d.K <= kFineK2;
+          const int gs = SPLIT ? group_slices(p, d.K) : 1;
+          const bool fine = SPLIT && gs == 0;
+          int kg = 0;  // slice within the current promotion group
           for (int kb = 0; kb < nk; ++kb) {
             if (!wait_bounded(full(st.idx), st.phase, p.error, abort, p.timeout_ns)) {
               ok = false;
@@ -331,8 +338,8 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
               }
               if (!ok) break;
             } else {
-              // a group spans kGroupKB2 slices; small products of each slice first
-              const bool first = (kb % kGroupKB2) == 0;
+              // a group spans gs slices; small products of each slice first
+              const bool first = kg == 0;
               if (first) {
                 if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
                   ok = false;
@@ -349,9 +356,10 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
               }
               for (int s = 0; s < s_end; ++s)
                 mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
-              if ((kb % kGroupKB2) == kGroupKB2 - 1 || kb == nk - 1) {
+              if (++kg == gs || kb == nk - 1) {
                 mma_commit_pair(tfull(acc.idx));
                 acc.next(kNAcc);
+                kg = 0;
               }
             }
             mma_commit_pair(empty(st.idx));
@@ -409,8 +417,8 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       }
       const int nk = (d.K + KE - 1) / KE;
       const int nsub = (d.K + KE / NSUB - 1) / (KE / NSUB);
-      const int ngroups = !SPLIT ? (nk > 0 ? 1 : 0)
-                          : (d.K <= kFineK2) ? nsub : (nk + kGroupKB2 - 1) / kGroupKB2;
+      const int gs = SPLIT ? group_slices(p, d.K) : 1;
+      const int ngroups = !SPLIT ? (nk > 0 ? 1 : 0) : gs == 0 ? nsub : (nk + gs - 1) / gs;
       float r[kCols];
 #pragma unroll
       for (int j = 0; j < kCols; ++j) r[j] = 0.0f;

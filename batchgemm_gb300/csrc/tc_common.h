@@ -29,6 +29,27 @@ __host__ __device__ constexpr bool tc_cfg_pair(int cfg) { return cfg >= kTcPairC
 __host__ __device__ constexpr int tc2_cfg_bn(int cfg) { return 64 << (cfg & 3); }
 __host__ __device__ constexpr bool tc2_cfg_valid(int cfg) { return (cfg & 3) != 3; }
 
+// Promotion schedule of the split modes on CTA pairs, per bucket of K:
+// bucket 0 is K <= 64, then one bucket per octave ((64, 128], (128, 256],
+// ..., (2048, 4096], above 4096).  group[b] = the number of 128-byte K
+// slices whose MMAs accumulate into one TMEM buffer before the epilogue adds
+// it into FP32 registers; 0 = promote after every MMA of K and keep the
+// lo*lo product too (the small-K path, where the split error dominates).
+constexpr int kTcSchedBuckets = 8;
+struct TcSchedule {
+  unsigned long long packed;  // byte b = group of bucket b (shifts, no indexing)
+  __host__ __device__ int group(int b) const { return (int)((packed >> (8 * b)) & 0xffu); }
+  __host__ __device__ void set(int b, int g) {
+    packed = (packed & ~(0xffull << (8 * b))) | ((unsigned long long)(g & 0xff) << (8 * b));
+  }
+};
+__host__ __device__ inline int tc_sched_bucket(int K) {
+  if (K <= 64) return 0;
+  int b = 0;
+  for (unsigned v = (unsigned)(K - 1) >> 6; v > 1u; v >>= 1) ++b;  // floor(log2(K-1)) - 6
+  return b + 1 < kTcSchedBuckets ? b + 1 : kTcSchedBuckets - 1;
+}
+
 // One pre-pass job: split/pack a strip of 32 rows of one operand.
 struct PackJob {
   int mat;
@@ -69,7 +90,11 @@ struct TcGemmParams {
   int* error;                  // bit 0: a bounded device wait expired
   unsigned long long timeout_ns;
   unsigned long long* cta_times;  // if set: [2 * blockIdx] start, [+1] end (global timer, ns)
+  TcSchedule sched;               // promotion groups of the split modes (pair kernel)
 };
+// The schedule the kernels use for a mode: the autotuned table, or a process-
+// wide override set through bgemm_debug_set_tc_schedule (the autotuner's sweep).
+TcSchedule tc_schedule(int mode);
 
 // Device-side construction of the per-matrix tensor maps: one warp per map
 // copies a host-encoded template, patches address, dims and row stride with

@@ -43,6 +43,20 @@ struct TcPlan {
 };
 
 static inline long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
+
+// ------------------------------------------------------ promotion schedule --
+static std::mutex g_sched_mu;
+static bool g_sched_override[3] = {false, false, false};
+static TcSchedule g_sched[3];
+
+TcSchedule tc_schedule(int mode) {
+  TcSchedule s{};
+  const int m = (mode >= BGEMM_MODE_TF32 && mode <= BGEMM_MODE_BF16X3) ? mode - 1 : 1;
+  std::lock_guard<std::mutex> lk(g_sched_mu);
+  if (g_sched_override[m]) return g_sched[m];
+  for (int b = 0; b < kTcSchedBuckets; ++b) s.set(b, kTcGroupTable[m][b]);
+  return s;
+}
 static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 static int g_mode = BGEMM_MODE_TF32X3;
@@ -384,9 +398,10 @@ bgemm_status_t tc_execute(bgemm_plan_s* p, float alpha, const float* const* dA,
                   t->kind,       t->split,      static_cast<char*>(t->d_ws), dA, dB};
   cudaError_t e = tc_pack_launch(pp, t->pack_grid, stream);
   if (e != cudaSuccess) return cuda_error(e, "split/pack launch");
-  TcGemmParams gp{p->d_descs, p->d_items, p->n_items, p->d_counters + kHdrItems,
-                  p->d_counters, t->d_tmaps, alpha, beta, dC, t->d_err, 2000000000ull,
-                  p->d_cta_times};
+  TcGemmParams gp{p->d_descs, p->d_items,  p->n_items, p->d_counters + kHdrItems,
+                  p->d_counters, t->d_tmaps, alpha,      beta,
+                  dC,            t->d_err,   2000000000ull, p->d_cta_times,
+                  tc_schedule(p->mode)};
   if (p->ev_start) cudaEventRecord(p->ev_start, stream);
   e = t->pair ? tc2_gemm_launch(t->kind, t->split, gp, p->grid, stream)
               : tc_gemm_launch(t->kind, t->split, gp, p->grid, stream);
@@ -458,5 +473,28 @@ extern "C" int bgemm_debug_bounded_wait_selftest(unsigned long long limit_ns, in
   if (error) *error = h[0];
   if (returned) *returned = h[1];
   if (wait_ok) *wait_ok = h[2];
+  return 0;
+}
+
+extern "C" int bgemm_debug_set_tc_schedule(int mode, const int* group) {
+  using namespace bgemm;
+  if (mode < BGEMM_MODE_TF32 || mode > BGEMM_MODE_BF16X3) return -1;
+  std::lock_guard<std::mutex> lk(g_sched_mu);
+  if (!group) {
+    g_sched_override[mode - 1] = false;
+    return 0;
+  }
+  for (int b = 0; b < kTcSchedBuckets; ++b)
+    if (group[b] < 0 || group[b] > 64) return -1;
+  for (int b = 0; b < kTcSchedBuckets; ++b) g_sched[mode - 1].set(b, group[b]);
+  g_sched_override[mode - 1] = true;
+  return 0;
+}
+
+extern "C" int bgemm_debug_get_tc_schedule(int mode, int* group) {
+  using namespace bgemm;
+  if (mode < BGEMM_MODE_TF32 || mode > BGEMM_MODE_BF16X3 || !group) return -1;
+  const TcSchedule s = tc_schedule(mode);
+  for (int b = 0; b < kTcSchedBuckets; ++b) group[b] = s.group(b);
   return 0;
 }

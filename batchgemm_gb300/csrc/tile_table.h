@@ -58,4 +58,15 @@ constexpr TileCost kTcCost[3][16] = {
 #undef BGEMM_TC1
 #endif
 
+// Promotion schedule of the split tensor-core modes on CTA pairs, indexed
+// [mode - 1][bucket of K] (see TcSchedule in tc_common.h): 128-byte K slices
+// per promotion group, 0 = promote every MMA of K and keep lo*lo.  The
+// single-product TF32 row is unused.  Defaults: the small-K path up to
+// K = 64, groups of two slices above; the autotuner replaces them with the
+// fastest groups whose error against FP64 stays within the FP32 SIMT path's.
+#if !defined(BGEMM_TUNED_HAS_SCHEDULE)
+constexpr unsigned char kTcGroupTable[3][8] = {
+    {0, 2, 2, 2, 2, 2, 2, 2}, {0, 2, 2, 2, 2, 2, 2, 2}, {0, 2, 2, 2, 2, 2, 2, 2}};
+#endif
+
 }  // namespace bgemm

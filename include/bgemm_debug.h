@@ -94,6 +94,18 @@ int bgemm_debug_compare_tensor_maps(void* plan, void* stream, int* n_maps, int* 
 int bgemm_debug_bounded_wait_selftest(unsigned long long limit_ns, int* error, int* returned,
                                       int* wait_ok);
 
+/* Promotion schedule of the split tensor-core modes on CTA pairs (mode 2
+ * TF32X3, 3 BF16X3; 1 is accepted and unused): group[b] for the 8 buckets
+ * of K (K <= 64, then (64,128], (128,256], ..., (2048,4096], > 4096) is the
+ * number of 128-byte K slices accumulated in tensor memory before the
+ * epilogue promotes them into FP32 registers, 0 = promote every MMA and keep
+ * the lo*lo product.  bgemm_debug_set_tc_schedule overrides the autotuned
+ * table for every later launch in the process (NULL restores it; values
+ * above 64 are rejected); bgemm_debug_get_tc_schedule reads the schedule in
+ * use.  For the autotuner.  Return 0, or -1 on invalid arguments. */
+int bgemm_debug_set_tc_schedule(int mode, const int* group);
+int bgemm_debug_get_tc_schedule(int mode, int* group);
+
 /* Counters of the one-shot entries' plan cache on the current device:
  * entries and device bytes held, and since the process started: calls that
  * found their exact batch (hits), calls that re-planned a cached plan for

@@ -188,14 +188,13 @@ def test_pair_mode_chosen_for_large_matrices(cuda):
     run_mode("tf32x3", M[-4:], M[-4:], M[-4:], 1.0, 0.0, seed=12)
 
 
-def test_small_m_swapped_orientation(cuda):
-    # uneven-M shape class: tiny M, N = K = 1024 runs with the operands swapped
+@pytest.mark.parametrize("force", [None, 4, 5, 7, 12, 13, 14])
+def test_small_m_swapped_orientation(cuda, force):
+    """Uneven-M shape class (tiny M, N = K = 1024): the planner's own choice,
+    and every swapped configuration (C^T = B^T A^T, the long side on the MMA's
+    M dimension; one-SM 4, 5, 7 and CTA-pair 12, 13, 14) forced."""
     M = [1, 3, 16, 40, 64, 200]
-    p = bg.Plan(M, [1024] * 6, [1024] * 6, M, [1024] * 6, M, mode="tf32x3")
-    hist = p.info()["tile_config_hist"]
-    p.close()
-    assert sum(hist[4:8]) + sum(hist[12:16]) >= 4, hist  # swapped, one-SM or pair
-    run_mode("tf32x3", M, [1024] * 6, [1024] * 6, 1.0, 0.0, seed=9)
+    run_mode("tf32x3", M, [1024] * 6, [1024] * 6, 1.0, 0.0, seed=9, force=force)
 
 
 def test_tc_plan_graph_replay(cuda):

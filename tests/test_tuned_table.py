@@ -1,0 +1,71 @@
+"""The autotuned tables the planners and kernels compile in (csrc/
+tile_table_tuned.inc, written by batchgemm_gb300/autotune.py): shape and
+bounds, read back through the library's debug entries.  No GPU needed."""
+import ctypes
+import os
+import re
+
+import batchgemm_gb300 as bg
+from batchgemm_gb300 import autotune
+
+INC = os.path.join(os.path.dirname(bg.__file__), "csrc", "tile_table_tuned.inc")
+
+
+def test_schedule_table_shape_and_bounds(built_lib):
+    L = bg.lib()
+    text = open(INC).read()
+    m = re.search(r"kTcGroupTable\[3\]\[8\] = \{(.*)\};", text)
+    assert m, "the tuned table carries a promotion schedule"
+    rows = re.findall(r"\{([^{}]*)\}", m.group(1))
+    assert len(rows) == 3 and all(len(r.split(",")) == 8 for r in rows)
+    for mode in (2, 3):
+        g = (ctypes.c_int * 8)()
+        assert L.bgemm_debug_get_tc_schedule(mode, g) == 0
+        vals = list(g)
+        assert vals == [int(x) for x in rows[mode - 1].split(",")]
+        for b, v in enumerate(vals):
+            assert v in autotune.SCHED_CANDIDATES, (mode, b, v)
+            assert b <= 1 or v != 0, "the every-MMA path is only for K <= 128"
+
+
+def test_schedule_override_round_trip(built_lib):
+    L = bg.lib()
+    orig = (ctypes.c_int * 8)()
+    L.bgemm_debug_get_tc_schedule(2, orig)
+    try:
+        want = [0, 1, 2, 3, 4, 6, 8, 2]
+        assert L.bgemm_debug_set_tc_schedule(2, (ctypes.c_int * 8)(*want)) == 0
+        got = (ctypes.c_int * 8)()
+        L.bgemm_debug_get_tc_schedule(2, got)
+        assert list(got) == want
+        assert L.bgemm_debug_set_tc_schedule(2, (ctypes.c_int * 8)(*([99] * 8))) == -1
+        assert L.bgemm_debug_set_tc_schedule(7, (ctypes.c_int * 8)()) == -1
+    finally:
+        L.bgemm_debug_set_tc_schedule(2, None)
+    back = (ctypes.c_int * 8)()
+    L.bgemm_debug_get_tc_schedule(2, back)
+    assert list(back) == list(orig)
+
+
+def test_k_buckets():
+    """K <= 64, then one octave per bucket, capped at the last bucket."""
+    cases = {1: 0, 64: 0, 65: 1, 128: 1, 129: 2, 256: 2, 257: 3, 512: 3, 1024: 4, 1025: 5,
+             2048: 5, 4096: 6, 4097: 7, 100000: 7}
+    for K, b in cases.items():
+        assert autotune._bucket(K) == b, K
+    for b, K in enumerate(autotune.SCHED_BUCKET_K):
+        assert autotune._bucket(K) == b
+
+
+def test_cost_table_positive_for_every_runnable_configuration(built_lib):
+    L = bg.lib()
+    a, b = ctypes.c_float(), ctypes.c_float()
+    for c in range(8):
+        assert L.bgemm_debug_tile_cost(0, c, ctypes.byref(a), ctypes.byref(b)) == 0
+        assert a.value > 0 and b.value > 0
+    for mode in (1, 2, 3):
+        for c in range(16):
+            assert L.bgemm_debug_tile_cost(mode, c, ctypes.byref(a), ctypes.byref(b)) == 0
+            if c >= 8 and (c & 3) == 3:
+                continue  # no such CTA-pair tile
+            assert a.value > 0 and b.value > 0, (mode, c)
