@@ -290,6 +290,28 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
           const int gs = SPLIT ? group_slices(p, d.K) : 1;
           const bool fine = SPLIT && gs == 0;
           int kg = 0;  // slice within the current promotion group
+          // A 256-column buffer holds P = 256 / bn promotion groups side by
+          // side (sub-accumulators at column stride bn), so narrow tiles run P
+          // groups ahead before waiting on the epilogue's drain.
+          const int P = 256 / bn;
+          int sub = 0;        // promotion group within the current buffer
+          uint32_t gbuf = 0;  // TMEM address of the current group
+          auto begin_group = [&]() {
+            if (sub == 0) {
+              if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns))
+                return false;
+              tc_fence_after();
+            }
+            gbuf = tmem + acc.idx * 256u + (uint32_t)(sub * bn);
+            return true;
+          };
+          auto end_group = [&](bool last) {
+            if (++sub == P || last) {
+              mma_commit_pair(tfull(acc.idx));
+              acc.next(kNAcc);
+              sub = 0;
+            }
+          };
           for (int kb = 0; kb < nk; ++kb) {
             if (!wait_bounded(full(st.idx), st.phase, p.error, abort, p.timeout_ns)) {
               ok = false;
@@ -319,12 +341,11 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
               }
             } else if (fine) {
               for (int s = 0; s < s_end && ok; ++s) {
-                if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
+                if (!begin_group()) {
                   ok = false;
                   break;
                 }
-                tc_fence_after();
-                const uint32_t buf = tmem + acc.idx * 256u;
+                const uint32_t buf = gbuf;
                 // small K: the split error dominates, so lo*lo is kept too
                 mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + kB + 32u * s),
                                idesc, 0u);
@@ -333,21 +354,17 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
                 mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + kB + 32u * s), idesc,
                                1u);
                 mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
-                mma_commit_pair(tfull(acc.idx));
-                acc.next(kNAcc);
+                end_group(kb == nk - 1 && s == s_end - 1);
               }
               if (!ok) break;
             } else {
               // a group spans gs slices; small products of each slice first
               const bool first = kg == 0;
-              if (first) {
-                if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
-                  ok = false;
-                  break;
-                }
-                tc_fence_after();
+              if (first && !begin_group()) {
+                ok = false;
+                break;
               }
-              const uint32_t buf = tmem + acc.idx * 256u;
+              const uint32_t buf = gbuf;
               for (int s = 0; s < s_end; ++s) {
                 mma_pair<KIND>(buf, sw128_desc(sa + kA + 32u * s), sw128_desc(sb + 32u * s), idesc,
                                (first && s == 0) ? 0u : 1u);
@@ -357,8 +374,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
               for (int s = 0; s < s_end; ++s)
                 mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc, 1u);
               if (++kg == gs || kb == nk - 1) {
-                mma_commit_pair(tfull(acc.idx));
-                acc.next(kNAcc);
+                end_group(kb == nk - 1);
                 kg = 0;
               }
             }
@@ -428,25 +444,32 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       const int g_pf = BETA ? max(0, ngroups - kCPrefetchLead) : -1;
       if (BETA && ngroups == 0)
         c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
-      for (int g = 0; g < ngroups; ++g) {
-        if (BETA && g == g_pf)
-          c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
+      // buffers of up to P = 256 / bn promotion groups each (see the MMA lane);
+      // the groups are added in K order, as if each had a buffer of its own
+      const int P = SPLIT ? 256 / bn : 1;
+      for (int g0 = 0; g0 < ngroups; g0 += P) {
         if (lane == 0) ok = wait_bounded(tfull(acc.idx), acc.phase, p.error, abort, p.timeout_ns);
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (!ok) break;
         tc_fence_after();
-        const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + acc.idx * 256u + c_lo;
+        const int nsubs = min(P, ngroups - g0);
+        for (int sg = 0; sg < nsubs; ++sg) {
+          if (BETA && g0 + sg == g_pf)
+            c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
+          const uint32_t tb =
+              tmem + ((uint32_t)(q * 32) << 16) + acc.idx * 256u + (uint32_t)(sg * bn) + c_lo;
 #pragma unroll
-        for (int c = 0; c < kCols / 16; c += 2) {
-          if (c * 16 < ncols) {
-            float v0[16], v1[16];
-            tmem_ld16(tb + c * 16, v0);
-            tmem_ld16(tb + (c + 1) * 16, v1);
-            tmem_wait_ld();
+          for (int c = 0; c < kCols / 16; c += 2) {
+            if (c * 16 < ncols) {
+              float v0[16], v1[16];
+              tmem_ld16(tb + c * 16, v0);
+              tmem_ld16(tb + (c + 1) * 16, v1);
+              tmem_wait_ld();
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              r[c * 16 + j] += v0[j];
-              r[(c + 1) * 16 + j] += v1[j];
+              for (int j = 0; j < 16; ++j) {
+                r[c * 16 + j] += v0[j];
+                r[(c + 1) * 16 + j] += v1[j];
+              }
             }
           }
         }
