@@ -6,7 +6,10 @@
 //
 // Because the sizes live on the device, the tile queue is built there too:
 //   1. fw_plan_kernel (one CTA) picks each matrix's SIMT tile configuration
-//      with the same cost model as the host planner, buckets matrices by
+//      with the same cost model as the host planner, rebalances for
+//      parallelism (the host planner's rule, in rounds: a matrix whose tile
+//      is longer than the average load of a persistent CTA moves to smaller
+//      tiles when that lowers the makespan bound), buckets matrices by
 //      modelled tile time (quarter-octave bins) and reserves each matrix a
 //      contiguous range of the queue, longest tiles first;
 //   2. fw_expand_kernel writes the work items (one warp per matrix);
@@ -41,13 +44,26 @@ struct FwScratch {
 };
 
 // One matrix's tile configuration and bin (the same cost model as the host
-// planner); shared by fw_plan_kernel and its host replay.
+// planner); shared by fw_plan_kernel and its host replay.  Tile times are
+// formed with one fmaf and work is summed as 64-bit integer nanoseconds, so
+// the device and the host replay (on any CPU) make the same decisions.
 struct FwMat {
   int bad;    // size negative or above max_dim: skipped
   int cfg;    // -1: no output (M or N is 0, or skipped)
   int tiles;
   int bin;    // quarter-octave bin of the modelled tile time
 };
+
+__host__ __device__ inline long long fw_tiles(int M, int N, const SimtCfg& g) {
+  return (long long)((M + g.bm - 1) / g.bm) * ((N + g.bn - 1) / g.bn);
+}
+__host__ __device__ inline float fw_tile_ns(int K, const TileCost& c) {
+  return fmaf(c.b_ns, (float)K, c.a_ns);
+}
+__host__ __device__ inline long long fw_work(int M, int N, int K, int cfg, const SimtCfg* cfgs,
+                                             const TileCost* cost) {
+  return fw_tiles(M, N, cfgs[cfg]) * (long long)fw_tile_ns(K, cost[cfg]);
+}
 
 __host__ __device__ inline FwMat fw_plan_matrix(int M, int N, int K, int max_dim,
                                                 const SimtCfg* cfgs, const TileCost* cost) {
@@ -56,39 +72,102 @@ __host__ __device__ inline FwMat fw_plan_matrix(int M, int N, int K, int max_dim
   r.cfg = -1;
   if (!r.bad && M > 0 && N > 0) {
     double bw = 0.0;
-    float btt = 0.f;
     for (int c = kSimtNumCfgs - 1; c >= 0; --c) {
-      const long long t = (long long)((M + cfgs[c].bm - 1) / cfgs[c].bm) *
-                          ((N + cfgs[c].bn - 1) / cfgs[c].bn);
-      const float tt = cost[c].a_ns + cost[c].b_ns * (float)K;
-      const double w = (double)t * tt;
+      const long long t = fw_tiles(M, N, cfgs[c]);
+      const double w = (double)t * fw_tile_ns(K, cost[c]);
       if (r.cfg < 0 || w < bw * 0.999) {
         r.cfg = c;
         r.tiles = (int)t;
         bw = w;
-        btt = tt;
       }
     }
-    r.bin = min(kBins - 1, max(0, quarter_octave(btt) - 24));
   }
   return r;
 }
 
+// Rebalance step of one matrix on configuration `cfg` (the host planner's
+// rule, plan.cpp choose_tiles): if its tile is longer than the average load
+// W / slots of a persistent CTA, the configuration with shorter and more
+// tiles of least total work, if that lowers the makespan bound
+// max(W / slots, longest tile); else -1.
+__host__ __device__ inline int fw_rebalance(int M, int N, int K, int cfg, long long W,
+                                            long long slots, const SimtCfg* cfgs,
+                                            const TileCost* cost) {
+  const long long tt = (long long)fw_tile_ns(K, cost[cfg]);
+  if (tt * slots <= W) return -1;
+  const long long tiles = fw_tiles(M, N, cfgs[cfg]);
+  const long long w_old = tiles * tt;
+  int best = -1;
+  long long bw = 0, btt = 0;
+  for (int c = 0; c < kSimtNumCfgs; ++c) {
+    const long long t2 = (long long)fw_tile_ns(K, cost[c]);
+    const long long n2 = fw_tiles(M, N, cfgs[c]);
+    if (t2 >= tt || n2 <= tiles) continue;
+    const long long w = n2 * t2;
+    if (best < 0 || w < bw) {
+      best = c;
+      bw = w;
+      btt = t2;
+    }
+  }
+  if (best < 0) return -1;
+  const long long w_new = W - w_old + bw;
+  const long long before = W > tt * slots ? W : tt * slots;
+  const long long after = w_new > btt * slots ? w_new : btt * slots;
+  return after < before ? best : -1;
+}
+constexpr int kRebalanceRounds = 8;
+
 __global__ void fw_plan_kernel(const int* __restrict__ dM, const int* __restrict__ dN,
-                               const int* __restrict__ dK, int batch, int max_dim,
+                               const int* __restrict__ dK, int batch, int max_dim, int slots,
                                FwScratch s) {
   __shared__ int bin_tiles[kBins];
   __shared__ int bin_start[kBins];
+  __shared__ unsigned long long work, dwork;
+  __shared__ int changed;
   for (int b = threadIdx.x; b < kBins; b += blockDim.x) bin_tiles[b] = 0;
+  if (threadIdx.x == 0) work = 0;
   __syncthreads();
-  // per-matrix choice; the bin and offset are parked in mat_start for now
+  // per-matrix choice (mat_start: -1 no output, 0 has tiles, until the end)
   for (int i = threadIdx.x; i < batch; i += blockDim.x) {
     const int M = dM[i], N = dN[i], K = dK[i];
     const FwMat r = fw_plan_matrix(M, N, K, max_dim, c_cfgs, c_cost);
     if (r.bad) atomicOr(s.err, 1);
-    s.descs[i] = MatDesc{M, N, K, max(M, 1), max(K, 1), max(M, 1), r.cfg < 0 ? 0 : r.cfg,
-                         r.cfg < 0 ? 0 : r.bin};
-    s.mat_start[i] = r.cfg < 0 ? -1 : atomicAdd(&bin_tiles[r.bin], r.tiles);
+    s.descs[i] = MatDesc{M, N, K, max(M, 1), max(K, 1), max(M, 1), r.cfg < 0 ? 0 : r.cfg, 0};
+    s.mat_start[i] = r.cfg < 0 ? -1 : 0;
+    if (r.cfg >= 0) atomicAdd(&work, (unsigned long long)fw_work(M, N, K, r.cfg, c_cfgs, c_cost));
+  }
+  // parallelism rebalance in rounds, each against the round's starting total
+  for (int round = 0; round < kRebalanceRounds; ++round) {
+    __syncthreads();
+    const long long W = (long long)work;
+    if (threadIdx.x == 0) {
+      dwork = 0;
+      changed = 0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < batch; i += blockDim.x) {
+      if (s.mat_start[i] < 0) continue;
+      const MatDesc d = s.descs[i];
+      const int c2 = fw_rebalance(d.M, d.N, d.K, d.cfg, W, slots, c_cfgs, c_cost);
+      if (c2 < 0) continue;
+      atomicAdd(&dwork, (unsigned long long)(fw_work(d.M, d.N, d.K, c2, c_cfgs, c_cost) -
+                                            fw_work(d.M, d.N, d.K, d.cfg, c_cfgs, c_cost)));
+      s.descs[i].cfg = c2;
+      changed = 1;
+    }
+    __syncthreads();
+    if (!changed) break;
+    if (threadIdx.x == 0) work = (unsigned long long)W + dwork;
+  }
+  __syncthreads();
+  // bins of the final tile times; each matrix reserves its tiles in its bin
+  for (int i = threadIdx.x; i < batch; i += blockDim.x) {
+    if (s.mat_start[i] < 0) continue;
+    const MatDesc d = s.descs[i];
+    const int bin = min(kBins - 1, max(0, quarter_octave(fw_tile_ns(d.K, c_cost[d.cfg])) - 24));
+    s.descs[i].aux = bin;
+    s.mat_start[i] = atomicAdd(&bin_tiles[bin], (int)fw_tiles(d.M, d.N, c_cfgs[d.cfg]));
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -199,7 +278,8 @@ extern "C" bgemm_status_t bgemm_framework_gemm(const int* dM, const int* dN, con
     ctx.cap_batch = cb;
     ctx.cap_items = ci;
   }
-  fw_plan_kernel<<<1, 1024, 0, stream>>>(dM, dN, dK, batch, max_dim, ctx.s);
+  const int grid = df.num_sms * df.simt_ctas_per_sm;
+  fw_plan_kernel<<<1, 1024, 0, stream>>>(dM, dN, dK, batch, max_dim, grid, ctx.s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "framework plan kernel");
   fw_expand_kernel<<<(batch + 7) / 8, 256, 0, stream>>>(batch, ctx.s);
@@ -207,7 +287,7 @@ extern "C" bgemm_status_t bgemm_framework_gemm(const int* dM, const int* dN, con
   if (e != cudaSuccess) return cuda_error(e, "framework expand kernel");
   SimtParams sp{ctx.s.descs, ctx.s.items, 0, ctx.s.n_items, ctx.s.counters, 1.0f, 1.0f,
                 const_cast<const float* const*>(dA), const_cast<const float* const*>(dB), dC};
-  e = simt_launch(sp, df.num_sms * df.simt_ctas_per_sm, stream);
+  e = simt_launch(sp, grid, stream);
   if (e != cudaSuccess) return cuda_error(e, "framework SIMT launch");
   return BGEMM_SUCCESS;
 }
@@ -254,7 +334,7 @@ cudaError_t fw_launch_on_scratch(const int* dM, const int* dN, const int* dK, fl
       ctx.consts = true;
     }
   }
-  fw_plan_kernel<<<1, 1024, 0, stream>>>(dM, dN, dK, batch, max_dim, s);
+  fw_plan_kernel<<<1, 1024, 0, stream>>>(dM, dN, dK, batch, max_dim, grid, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   fw_expand_kernel<<<(batch + 7) / 8, 256, 0, stream>>>(batch, s);
@@ -306,23 +386,46 @@ extern "C" bgemm_status_t bgemm_framework_check_device(bgemm_stream_t stream) {
 }
 
 // Host replay of fw_plan_kernel + fw_expand_kernel (tests without a GPU): the
-// same per-matrix choices, reserved in matrix order instead of by atomics.
+// same per-matrix choices and rebalance rounds, reserved in matrix order
+// instead of by atomics; `slots` is the persistent SIMT grid the entry uses.
 extern "C" int bgemm_debug_framework_plan(const int* M, const int* N, const int* K, int batch,
-                                          int max_dim, int* cfg_out, int* items_out,
+                                          int max_dim, int slots, int* cfg_out, int* items_out,
                                           int max_items, int* err) {
-  if (batch < 0 || !err || (batch > 0 && (!M || !N || !K))) return -1;
-  std::vector<FwMat> r(batch);
+  if (batch < 0 || !err || slots < 1 || (batch > 0 && (!M || !N || !K))) return -1;
+  std::vector<int> cfg(batch, -1);
   std::vector<int> start(batch, -1);
   int bin_tiles[kBins] = {};
   *err = 0;
+  long long W = 0;
   for (int i = 0; i < batch; ++i) {
-    r[i] = fw_plan_matrix(M[i], N[i], K[i], max_dim, kSimtCfgs, kSimtCost);
-    if (r[i].bad) *err |= 1;
-    if (cfg_out) cfg_out[i] = r[i].cfg;
-    if (r[i].cfg >= 0) {
-      start[i] = bin_tiles[r[i].bin];
-      bin_tiles[r[i].bin] += r[i].tiles;
+    const FwMat r = fw_plan_matrix(M[i], N[i], K[i], max_dim, kSimtCfgs, kSimtCost);
+    if (r.bad) *err |= 1;
+    cfg[i] = r.cfg;
+    if (r.cfg >= 0) W += fw_work(M[i], N[i], K[i], r.cfg, kSimtCfgs, kSimtCost);
+  }
+  for (int round = 0; round < kRebalanceRounds; ++round) {
+    long long dW = 0;
+    bool changed = false;
+    for (int i = 0; i < batch; ++i) {
+      if (cfg[i] < 0) continue;
+      const int c2 = fw_rebalance(M[i], N[i], K[i], cfg[i], W, slots, kSimtCfgs, kSimtCost);
+      if (c2 < 0) continue;
+      dW += fw_work(M[i], N[i], K[i], c2, kSimtCfgs, kSimtCost) -
+            fw_work(M[i], N[i], K[i], cfg[i], kSimtCfgs, kSimtCost);
+      cfg[i] = c2;
+      changed = true;
     }
+    if (!changed) break;
+    W += dW;
+  }
+  std::vector<int> bin(batch, 0);
+  for (int i = 0; i < batch; ++i) {
+    if (cfg_out) cfg_out[i] = cfg[i];
+    if (cfg[i] < 0) continue;
+    bin[i] = std::min(kBins - 1,
+                      std::max(0, quarter_octave(fw_tile_ns(K[i], kSimtCost[cfg[i]])) - 24));
+    start[i] = bin_tiles[bin[i]];
+    bin_tiles[bin[i]] += (int)fw_tiles(M[i], N[i], kSimtCfgs[cfg[i]]);
   }
   int bin_start[kBins], n = 0;
   for (int b = kBins - 1; b >= 0; --b) {
@@ -332,9 +435,9 @@ extern "C" int bgemm_debug_framework_plan(const int* M, const int* N, const int*
   if (items_out && n > max_items) return -1;
   for (int i = 0; items_out && i < batch; ++i) {
     if (start[i] < 0) continue;
-    const int tmx = (M[i] + kSimtCfgs[r[i].cfg].bm - 1) / kSimtCfgs[r[i].cfg].bm;
-    const int tnx = (N[i] + kSimtCfgs[r[i].cfg].bn - 1) / kSimtCfgs[r[i].cfg].bn;
-    const int s0 = bin_start[r[i].bin] + start[i];
+    const int tmx = (M[i] + kSimtCfgs[cfg[i]].bm - 1) / kSimtCfgs[cfg[i]].bm;
+    const int tnx = (N[i] + kSimtCfgs[cfg[i]].bn - 1) / kSimtCfgs[cfg[i]].bn;
+    const int s0 = bin_start[bin[i]] + start[i];
     for (int t = 0; t < tmx * tnx; ++t) {
       items_out[3 * (s0 + t)] = i;
       items_out[3 * (s0 + t) + 1] = t % tmx;

@@ -49,13 +49,15 @@ constexpr int kA = kRows * 128;            // 16 KB per part
 constexpr int kB = 128 * 128;              // B-side half: up to 128 rows
 constexpr int kNAcc = 2;                   // 256-column accumulator buffers
 constexpr int kSched = 4;                  // schedule slots (items published ahead)
-// Stage ring: split modes hold hi + lo of both sides (64 KB, 3 stages), the
-// single-product TF32 mode hi only (32 KB, 6 stages).
+// Stage ring of 3 stages of 64 KB, two parts per side: the split modes' hi and
+// lo halves of one 128-byte K slice, or two consecutive K slices of the
+// single-product TF32 mode (four TMA boxes per stage either way: one thread
+// keeps ~150 GB/s per SM in flight with four boxes per stage, ~100 with two).
 template <int SPLIT>
 struct Geo2 {
-  static constexpr int NP = SPLIT ? 2 : 1;
+  static constexpr int NP = 2;
   static constexpr int STAGE = NP * (kA + kB);
-  static constexpr int S = SPLIT ? 3 : 6;
+  static constexpr int S = 3;
   static constexpr int NBAR = 2 * S + 2 * kNAcc + 1 + 2 * kSched;
   // barriers | TMEM address, abort flag (16 B) | schedule slots | alignment
   static constexpr int SMEM = S * STAGE + NBAR * 8 + 16 + 4 * kSched + 1024;
@@ -229,11 +231,14 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
             for (int q = 0; q < 4; ++q) tmap_acquire(tm + q);
             last_mat = ti.mat;
           }
-          const int nk = (d.K + KE - 1) / KE;
-          const uint32_t tx = 2u * G::NP * (uint32_t)(kA + hb * 128);  // both CTAs, all parts
+          const int nk = (d.K + KE - 1) / KE;           // 128-byte K slices
+          const int nst = SPLIT ? nk : (nk + 1) / 2;     // stages
           const int row_a = ti.tm * 256 + (int)rank * kRows;
           const int row_b = ti.tn * bn + (int)rank * (tile_n(d, ti.tn, bn) >> 1);
-          for (int kb = 0; kb < nk; ++kb) {
+          for (int kb = 0; kb < nst; ++kb) {
+            // single product: slices 2kb and (if it exists) 2kb + 1
+            const int parts = SPLIT ? 2 : (2 * kb + 1 < nk ? 2 : 1);
+            const uint32_t tx = 2u * parts * (uint32_t)(kA + hb * 128);  // both CTAs
             if (!wait_bounded(empty(st.idx), st.phase ^ 1u, p.error, abort, p.timeout_ns)) {
               ok = false;
               break;
@@ -246,11 +251,16 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
               inflight |= 1u << st.idx;
               inflight_phase = (inflight_phase & ~(1u << st.idx)) | (st.phase << st.idx);
             }
-            tma_load_2d_pair(sa, tm + 0, kb * KE, row_a, fb);
-            tma_load_2d_pair(sb, tm + 2, kb * KE, row_b, fb);
             if (SPLIT) {
+              tma_load_2d_pair(sa, tm + 0, kb * KE, row_a, fb);
+              tma_load_2d_pair(sb, tm + 2, kb * KE, row_b, fb);
               tma_load_2d_pair(sa + kA, tm + 1, kb * KE, row_a, fb);
               tma_load_2d_pair(sb + kB, tm + 3, kb * KE, row_b, fb);
+            } else {
+              for (int j = 0; j < parts; ++j) {
+                tma_load_2d_pair(sa + j * kA, tm + 0, (2 * kb + j) * KE, row_a, fb);
+                tma_load_2d_pair(sb + j * kB, tm + 2, (2 * kb + j) * KE, row_b, fb);
+              }
             }
             st.next(kS);
           }
@@ -312,7 +322,8 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
               sub = 0;
             }
           };
-          for (int kb = 0; kb < nk; ++kb) {
+          const int nst = SPLIT ? nk : (nk + 1) / 2;  // stages (the producer's count)
+          for (int kb = 0; kb < nst; ++kb) {
             if (!wait_bounded(full(st.idx), st.phase, p.error, abort, p.timeout_ns)) {
               ok = false;
               break;
@@ -323,7 +334,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
             const int s_end = min(NSUB, nsub - kb * NSUB);
             if (!SPLIT) {
               // one product: a single accumulator per tile, the 2-deep ring
-              // alternating between tiles
+              // alternating between tiles; the stage holds K slices 2kb, 2kb+1
               if (kb == 0) {
                 if (!wait_bounded(tempty(acc.idx), acc.phase ^ 1u, p.error, abort, p.timeout_ns)) {
                   ok = false;
@@ -332,10 +343,15 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
                 tc_fence_after();
               }
               const uint32_t buf = tmem + acc.idx * 256u;
-              for (int s = 0; s < s_end; ++s)
-                mma_pair<KIND>(buf, sw128_desc(sa + 32u * s), sw128_desc(sb + 32u * s), idesc,
-                               (kb > 0 || s > 0) ? 1u : 0u);
-              if (kb == nk - 1) {
+              for (int j = 0; j < 2 && 2 * kb + j < nk; ++j) {
+                const int slice = 2 * kb + j;
+                const int se = min(NSUB, nsub - slice * NSUB);
+                for (int s = 0; s < se; ++s)
+                  mma_pair<KIND>(buf, sw128_desc(sa + j * kA + 32u * s),
+                                 sw128_desc(sb + j * kB + 32u * s), idesc,
+                                 (slice > 0 || s > 0) ? 1u : 0u);
+              }
+              if (kb == nst - 1) {
                 mma_commit_pair(tfull(acc.idx));
                 acc.next(kNAcc);
               }

@@ -43,13 +43,14 @@ int bgemm_debug_tc_plan(const int* M, const int* N, const int* K, int batch, int
                         int* n_jobs, long long* ws_bytes, int* kernel_family);
 
 /* Host replay of the planner that bgemm_framework_gemm runs on the device
- * (same per-matrix SIMT tile choice and bins, reserved in matrix order).
+ * (same per-matrix SIMT tile choice, parallelism rebalance rounds for
+ * `slots` persistent CTAs, and bins, reserved in matrix order).
  * cfg_out[batch]: tile configuration (-1: no output); items_out
  * [3*max_items]: (matrix, tile along M, tile along N) in queue order; *err:
  * bit 0 when a size is negative or above max_dim.  Returns the number of work
  * items, or -1 on invalid arguments or too small output arrays. */
 int bgemm_debug_framework_plan(const int* M, const int* N, const int* K, int batch, int max_dim,
-                               int* cfg_out, int* items_out, int max_items, int* err);
+                               int slots, int* cfg_out, int* items_out, int max_items, int* err);
 
 /* Host replay of the planner that bgemm_framework_gemm_mode runs on the
  * device (same per-matrix tile choice, bins and reservations, made in matrix

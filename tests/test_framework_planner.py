@@ -192,7 +192,10 @@ def test_device_planner_replay_prefers_pair_tiles_of_the_cost_table(built_lib):
 SIMT_CFGS = [(16, 16), (32, 32), (64, 32), (32, 64), (64, 64), (128, 64), (64, 128), (128, 128)]
 
 
-def fw_simt_plan(M, N, K, max_dim):
+SLOTS = 304  # persistent SIMT CTAs on GB300 (152 SMs x 2)
+
+
+def fw_simt_plan(M, N, K, max_dim, slots=SLOTS):
     L = bg.lib()
     n = len(M)
     ia = lambda v: (ctypes.c_int * max(n, 1))(*v)
@@ -200,10 +203,10 @@ def fw_simt_plan(M, N, K, max_dim):
     f.restype = ctypes.c_int
     cfg = (ctypes.c_int * max(n, 1))()
     err = ctypes.c_int()
-    cnt = f(ia(M), ia(N), ia(K), n, max_dim, cfg, None, 0, ctypes.byref(err))
+    cnt = f(ia(M), ia(N), ia(K), n, max_dim, slots, cfg, None, 0, ctypes.byref(err))
     assert cnt >= 0
     items = (ctypes.c_int * max(3 * cnt, 1))()
-    assert f(ia(M), ia(N), ia(K), n, max_dim, cfg, items, cnt, ctypes.byref(err)) == cnt
+    assert f(ia(M), ia(N), ia(K), n, max_dim, slots, cfg, items, cnt, ctypes.byref(err)) == cnt
     return list(cfg)[:n], np.array(items[:3 * cnt]).reshape(-1, 3), err.value
 
 
@@ -241,3 +244,23 @@ def test_quarter_octave_bins_match_log2(built_lib):
         v = 4 * math.log2(float(x32))
         if abs(v - round(v)) > 1e-5:
             assert quarter_octave(x32) == math.floor(v), x32
+
+
+def test_simt_device_planner_rebalances_small_batches(built_lib):
+    """The reference's small sweep batches (first 8 or 16 rows of its shape
+    file): with one wave of persistent CTAs the rebalance splits the longest
+    tiles, so the queue holds more, shorter tiles than the per-matrix choice
+    alone; a batch with plenty of tiles is left alone."""
+    from batchgemm_gb300 import workloads
+    for B in (8, 16):
+        w = workloads.ref_dataset(B)
+        _, items_1, _ = fw_simt_plan(w.M, w.N, w.K, 512, slots=1)   # one CTA: no split helps
+        cfgs, items, err = fw_simt_plan(w.M, w.N, w.K, 512)
+        assert err == 0 and len(items) > len(items_1), (B, len(items), len(items_1))
+        assert_longest_first(items, cfgs, w.K, 0)
+    rng = np.random.default_rng(9)
+    M = rng.integers(256, 1024, 600).tolist()
+    _, a, _ = fw_simt_plan(M, M, M, 1024, slots=1)
+    _, b, _ = fw_simt_plan(M, M, M, 1024)
+    assert len(a) == len(b)  # thousands of tiles for 304 CTAs: nothing to rebalance
+

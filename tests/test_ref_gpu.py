@@ -146,22 +146,27 @@ def test_reference_kernel_timing(ref_kernel):
           % (t_ref, flops / t_ref / 1e9, t_ours, flops / t_ours / 1e9))
 
 
-def _time(fn, reps=10, sync_each=False):
-    """Mean ms of `reps` calls after one warm-up, CUDA events on the current
-    stream; sync_each mirrors the reference's timed loop, which synchronises
-    the device after every launch (CUDA/framework/gemm.cu:203-214)."""
+def _time(fn, reps=20, rounds=5, sync_each=False):
+    """Median over `rounds` of the mean ms of `reps` calls (after a warm-up),
+    CUDA events on the current stream; sync_each mirrors the reference's timed
+    loop, which synchronises the device after every launch
+    (CUDA/framework/gemm.cu:203-214).  Calls of tens of microseconds vary a
+    lot from one round to the next, hence the median."""
     fn()
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(reps):
-        fn()
-        if sync_each:
-            torch.cuda.synchronize()
-    e1.record()
-    torch.cuda.synchronize()
-    return e0.elapsed_time(e1) / reps
+    out = []
+    for _ in range(rounds):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+            if sync_each:
+                torch.cuda.synchronize()
+        e1.record()
+        torch.cuda.synchronize()
+        out.append(e0.elapsed_time(e1) / reps)
+    return sorted(out)[len(out) // 2]
 
 
 def test_reference_sweep_table(ref_kernel):
