@@ -64,16 +64,16 @@ class PlanRequirements(ctypes.Structure):
     """bgemm_plan_requirements_t: device sizes of a batch inside a plan."""
     _fields_ = [("batch", ctypes.c_int), ("tiles", ctypes.c_int), ("pack_jobs", ctypes.c_int),
                 ("kernel_family", ctypes.c_int), ("workspace_bytes", ctypes.c_size_t),
-                ("reserved", ctypes.c_int * 4)]
+                ("simt_tiles", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+    KEYS = ("batch", "tiles", "pack_jobs", "kernel_family", "workspace_bytes", "simt_tiles")
 
     def as_dict(self):
-        return {"batch": self.batch, "tiles": self.tiles, "pack_jobs": self.pack_jobs,
-                "kernel_family": self.kernel_family, "workspace_bytes": self.workspace_bytes}
+        return {k: getattr(self, k) for k in self.KEYS}
 
     @classmethod
     def from_dict(cls, d):
         r = cls()
-        for k in ("batch", "tiles", "pack_jobs", "kernel_family", "workspace_bytes"):
+        for k in cls.KEYS:
             setattr(r, k, int(d.get(k, 0)))
         return r
 
@@ -86,7 +86,8 @@ class PlanOptions(ctypes.Structure):
                 ("disable_rebalance", ctypes.c_int), ("host_tensor_maps", ctypes.c_int),
                 ("kernel_family", ctypes.c_int),
                 ("layout", ctypes.c_int), ("trans_a", ctypes.c_int), ("trans_b", ctypes.c_int),
-                ("reserved", ctypes.c_int * 3), ("capacity", PlanRequirements)]
+                ("simt_below", ctypes.c_int), ("reserved", ctypes.c_int * 2),
+                ("capacity", PlanRequirements)]
 
 
 LAYOUTS = {"col": 0, "row": 1}
@@ -104,8 +105,9 @@ def _op(v) -> int:
 
 def _options(force_tile_config=-1, max_ctas=0, rebalance=True, host_tensor_maps=False,
              kernel_family="auto", capacity=None, layout="col",
-             trans_a=False, trans_b=False) -> PlanOptions:
+             trans_a=False, trans_b=False, simt_below=0) -> PlanOptions:
     opt = PlanOptions()
+    opt.simt_below = int(simt_below)
     opt.layout = _layout(layout)
     opt.trans_a = _op(trans_a)
     opt.trans_b = _op(trans_b)
@@ -244,7 +246,7 @@ def plan_requirements(M, N, K, lda, ldb, ldc, mode="simt", **options) -> dict:
 
 def max_requirements(reqs) -> dict:
     """Element-wise maximum of requirement dicts (a capacity for all of them)."""
-    out = {"batch": 0, "tiles": 0, "pack_jobs": 0, "kernel_family": 0, "workspace_bytes": 0}
+    out = {k: 0 for k in PlanRequirements.KEYS}
     for r in reqs:
         for k in out:
             out[k] = max(out[k], int(r[k]))
@@ -265,12 +267,12 @@ class Plan:
 
     def __init__(self, M, N, K, lda, ldb, ldc, mode="simt", stream=None,
                  force_tile_config: int = -1, max_ctas: int = 0, rebalance: bool = True,
-                 host_tensor_maps: bool = False, kernel_family="auto", capacity=None, layout="col", trans_a=False,
-                 trans_b=False):
+                 host_tensor_maps: bool = False, kernel_family="auto", capacity=None,
+                 layout="col", trans_a=False, trans_b=False, simt_below: int = 0):
         self._h = ctypes.c_void_p()
         self.batch = len(M)
         opt = _options(force_tile_config, max_ctas, rebalance, host_tensor_maps,
-                       kernel_family, capacity, layout, trans_a, trans_b)
+                       kernel_family, capacity, layout, trans_a, trans_b, simt_below)
         _check(lib().bgemm_plan_create_ex(ctypes.byref(self._h), _iarr(M), _iarr(N), _iarr(K),
                                           _iarr(lda), _iarr(ldb), _iarr(ldc), len(M),
                                           _mode(mode), _stream(stream), ctypes.byref(opt)))

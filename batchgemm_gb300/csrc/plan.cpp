@@ -509,11 +509,95 @@ static bgemm_status_t plan_batch_oriented(bgemm_plan_s* p, const int* M, const i
   return plan_batch(p, M, N, K, lda, ldb, ldc, batch, first, bp);
 }
 
+// ------------------------------------------------------------ mixed plans --
+bgemm_status_t plan_create(bgemm_plan_t* out, const int* M, const int* N, const int* K,
+                           const int* lda, const int* ldb, const int* ldc, int batch, int mode,
+                           cudaStream_t stream, const bgemm_plan_options_t* opt);
+bgemm_status_t plan_update(bgemm_plan_t p, const int* M, const int* N, const int* K,
+                           const int* lda, const int* ldb, const int* ldc, int batch,
+                           cudaStream_t stream);
+bgemm_status_t plan_requirements(const int* M, const int* N, const int* K, const int* lda,
+                                 const int* ldb, const int* ldc, int batch, int mode,
+                                 const bgemm_plan_options_t* opt,
+                                 bgemm_plan_requirements_t* out);
+bgemm_status_t plan_destroy(bgemm_plan_t p);
+
+// M of the matrices that run on the SIMT kernel (simt = true) or on the
+// tensor cores (simt = false); the others get M = 0, which both planners
+// treat as an empty matrix (no tiles, no pre-pass jobs, pointers not read).
+static std::vector<int> mixed_mask(const int* M, const int* N, const int* K, int batch,
+                                   int below, bool simt) {
+  std::vector<int> m((size_t)std::max(batch, 1), 0);
+  for (int i = 0; i < batch; ++i) {
+    const bool small = std::min(M[i], std::min(N[i], K[i])) < below;
+    m[i] = (small == simt) ? M[i] : 0;
+  }
+  return m;
+}
+
+static void mixed_info(bgemm_plan_s* p) {
+  const bgemm_plan_info_t& a = p->mix_simt->info;
+  const bgemm_plan_info_t& b = p->mix_tc->info;
+  p->info = b;
+  p->info.batch = p->batch;
+  p->info.num_tiles = p->mix_simt->n_items + p->mix_tc->n_items;
+  p->info.useful_flops = a.useful_flops + b.useful_flops;
+  p->info.min_bytes = a.min_bytes + b.min_bytes;
+  p->info.device_bytes = a.device_bytes + b.device_bytes;
+  p->info.kernels_per_execute = a.kernels_per_execute + b.kernels_per_execute;
+}
+
+static bgemm_status_t plan_create_mixed(bgemm_plan_t* out, const int* M, const int* N,
+                                        const int* K, const int* lda, const int* ldb,
+                                        const int* ldc, int batch, int mode, cudaStream_t stream,
+                                        const bgemm_plan_options_t* opt) {
+  bgemm_plan_options_t o = *opt;
+  o.simt_below = 0;
+  bgemm_plan_options_t os = o;
+  os.capacity = bgemm_plan_requirements_t{};
+  os.capacity.batch = opt->capacity.batch;
+  os.capacity.tiles = opt->capacity.simt_tiles;
+  bgemm_plan_options_t ot = o;
+  ot.capacity.simt_tiles = 0;
+  const std::vector<int> ms = mixed_mask(M, N, K, batch, opt->simt_below, true);
+  const std::vector<int> mt = mixed_mask(M, N, K, batch, opt->simt_below, false);
+  bgemm_plan_t ps = nullptr, pt = nullptr;
+  bgemm_status_t st = plan_create(&ps, ms.data(), N, K, lda, ldb, ldc, batch,
+                                  BGEMM_MODE_SIMT_FP32, stream, &os);
+  if (st == BGEMM_SUCCESS)
+    st = plan_create(&pt, mt.data(), N, K, lda, ldb, ldc, batch, mode, stream, &ot);
+  if (st != BGEMM_SUCCESS) {
+    plan_destroy(ps);
+    return st;
+  }
+  auto* p = new bgemm_plan_s();
+  p->mode = mode;
+  p->batch = batch;
+  p->facts = pt->facts;
+  p->opt = *opt;
+  p->mix_simt = ps;
+  p->mix_tc = pt;
+  p->cap = pt->cap;
+  p->cap.simt_tiles = ps->cap.tiles;
+  p->grid = pt->grid;
+  mixed_info(p);
+  *out = p;
+  return BGEMM_SUCCESS;
+}
+
 bgemm_status_t plan_create(bgemm_plan_t* out, const int* M, const int* N, const int* K,
                            const int* lda, const int* ldb, const int* ldc, int batch, int mode,
                            cudaStream_t stream, const bgemm_plan_options_t* opt) {
   if (!out) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
   *out = nullptr;
+  if (opt && opt->simt_below < 0)
+    return set_error(BGEMM_ERROR_INVALID_VALUE, 11, -1, "simt_below %d < 0", opt->simt_below);
+  if (opt && opt->simt_below > 0 && mode != BGEMM_MODE_SIMT_FP32) {
+    bgemm_status_t st = check_args(M, N, K, lda, ldb, ldc, batch, mode, 2, 3, 4, 5, 6, 7, 8, 9,
+                                   opt->layout == 1, opt->trans_a != 0, opt->trans_b != 0);
+    if (st != BGEMM_SUCCESS) return st;
+    return plan_create_mixed(out, M, N, K, lda, ldb, ldc, batch, mode, stream, opt);
+  }
   bgemm_plan_s probe;
   probe.opt = opt ? *opt : default_options();
   bgemm_status_t st = set_orientation(&probe, 11);
@@ -559,6 +643,38 @@ bgemm_status_t plan_update(bgemm_plan_t p, const int* M, const int* N, const int
                            const int* lda, const int* ldb, const int* ldc, int batch,
                            cudaStream_t stream) {
   if (!p) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
+  if (p->mix_tc) {
+    bgemm_status_t st = check_args(M, N, K, lda, ldb, ldc, batch, p->mode, 2, 3, 4, 5, 6, 7, 8,
+                                   8, p->opt.layout == 1, p->opt.trans_a != 0,
+                                   p->opt.trans_b != 0);
+    if (st != BGEMM_SUCCESS) return st;
+    const std::vector<int> ms = mixed_mask(M, N, K, batch, p->opt.simt_below, true);
+    const std::vector<int> mt = mixed_mask(M, N, K, batch, p->opt.simt_below, false);
+    // both children check their capacity before they change anything
+    bgemm_plan_requirements_t rs{}, rt{};
+    bgemm_plan_options_t o = p->opt;
+    o.simt_below = 0;
+    st = plan_requirements(ms.data(), N, K, lda, ldb, ldc, batch, BGEMM_MODE_SIMT_FP32, &o, &rs);
+    if (st == BGEMM_SUCCESS)
+      st = plan_requirements(mt.data(), N, K, lda, ldb, ldc, batch, p->mode, &o, &rt);
+    if (st != BGEMM_SUCCESS) return st;
+    if (batch > p->cap.batch || rs.tiles > p->mix_simt->cap.tiles ||
+        rt.tiles > p->mix_tc->cap.tiles || rt.pack_jobs > p->mix_tc->cap.pack_jobs ||
+        rt.workspace_bytes > p->mix_tc->cap.workspace_bytes)
+      return set_error(BGEMM_ERROR_NOT_SUPPORTED, 0, -1,
+                       "batch needs %d SIMT tiles, %d tensor-core tiles, %d pack jobs, %zu "
+                       "workspace bytes; the mixed plan holds %d, %d, %d, %zu",
+                       rs.tiles, rt.tiles, rt.pack_jobs, rt.workspace_bytes,
+                       p->mix_simt->cap.tiles, p->mix_tc->cap.tiles, p->mix_tc->cap.pack_jobs,
+                       p->mix_tc->cap.workspace_bytes);
+    st = plan_update(p->mix_simt, ms.data(), N, K, lda, ldb, ldc, batch, stream);
+    if (st == BGEMM_SUCCESS)
+      st = plan_update(p->mix_tc, mt.data(), N, K, lda, ldb, ldc, batch, stream);
+    if (st != BGEMM_SUCCESS) return st;
+    p->batch = batch;
+    mixed_info(p);
+    return BGEMM_SUCCESS;
+  }
   bgemm_status_t st =
       check_args(M, N, K, lda, ldb, ldc, batch, p->mode, 2, 3, 4, 5, 6, 7, 8, 8, p->row_major,
                  p->opt.trans_a != 0, p->opt.trans_b != 0);
@@ -594,6 +710,24 @@ bgemm_status_t plan_requirements(const int* M, const int* N, const int* K, const
                                  const int* ldb, const int* ldc, int batch, int mode,
                                  const bgemm_plan_options_t* opt,
                                  bgemm_plan_requirements_t* out) {
+  if (opt && opt->simt_below > 0 && mode != BGEMM_MODE_SIMT_FP32) {
+    if (!out) return set_error(BGEMM_ERROR_INVALID_VALUE, 10, -1, "out is NULL");
+    bgemm_status_t st = check_args(M, N, K, lda, ldb, ldc, batch, mode, 1, 2, 3, 4, 5, 6, 7, 8,
+                                   opt->layout == 1, opt->trans_a != 0, opt->trans_b != 0);
+    if (st != BGEMM_SUCCESS) return st;
+    bgemm_plan_options_t o = *opt;
+    o.simt_below = 0;
+    const std::vector<int> ms = mixed_mask(M, N, K, batch, opt->simt_below, true);
+    const std::vector<int> mt = mixed_mask(M, N, K, batch, opt->simt_below, false);
+    bgemm_plan_requirements_t rs{}, rt{};
+    st = plan_requirements(ms.data(), N, K, lda, ldb, ldc, batch, BGEMM_MODE_SIMT_FP32, &o, &rs);
+    if (st == BGEMM_SUCCESS) st = plan_requirements(mt.data(), N, K, lda, ldb, ldc, batch, mode,
+                                                    &o, &rt);
+    if (st != BGEMM_SUCCESS) return st;
+    *out = rt;
+    out->simt_tiles = rs.tiles;
+    return BGEMM_SUCCESS;
+  }
   bgemm_plan_s p;
   p.opt = opt ? *opt : default_options();
   bgemm_status_t st = set_orientation(&p, 9);
@@ -619,6 +753,13 @@ bgemm_status_t plan_execute(bgemm_plan_t p, float alpha, const float* const* dA,
                             const float* const* dB, float beta, float* const* dC,
                             cudaStream_t stream) {
   if (!p) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
+  if (p->mix_tc) {
+    // the matrices of the two children are disjoint: SIMT first, then the
+    // tensor-core pre-pass and GEMM, in stream order
+    bgemm_status_t st = plan_execute(p->mix_simt, alpha, dA, dB, beta, dC, stream);
+    if (st != BGEMM_SUCCESS) return st;
+    return plan_execute(p->mix_tc, alpha, dA, dB, beta, dC, stream);
+  }
   if (p->cap.tiles == 0) return BGEMM_SUCCESS;
   if (!dA) return set_error(BGEMM_ERROR_INVALID_VALUE, 3, -1, "dA is NULL");
   if (!dB) return set_error(BGEMM_ERROR_INVALID_VALUE, 4, -1, "dB is NULL");
@@ -643,6 +784,12 @@ bgemm_status_t plan_execute(bgemm_plan_t p, float alpha, const float* const* dA,
 
 bgemm_status_t plan_destroy(bgemm_plan_t p) {
   if (!p) return BGEMM_SUCCESS;
+  if (p->mix_tc) {
+    plan_destroy(p->mix_simt);
+    plan_destroy(p->mix_tc);
+    delete p;
+    return BGEMM_SUCCESS;
+  }
   free_plan_memory(p);
   delete p;
   return BGEMM_SUCCESS;
@@ -980,6 +1127,7 @@ bgemm_status_t bgemm_plan_set_cta_timer(bgemm_plan_t plan, void* d_times) {
   if (plan->mode == BGEMM_MODE_SIMT_FP32)
     return set_error(BGEMM_ERROR_NOT_SUPPORTED, 1, -1,
                      "per-CTA timing is a hook of the tensor-core GEMM kernels");
+  if (plan->mix_tc) plan = plan->mix_tc;
   plan->d_cta_times = static_cast<unsigned long long*>(d_times);
   return BGEMM_SUCCESS;
 }
@@ -987,6 +1135,7 @@ bgemm_status_t bgemm_plan_set_cta_timer(bgemm_plan_t plan, void* d_times) {
 bgemm_status_t bgemm_plan_set_kernel_events(bgemm_plan_t plan, void* ev_start, void* ev_stop) {
   clear_error();
   if (!plan) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
+  if (plan->mix_tc) plan = plan->mix_tc;  // the tensor-core GEMM, the dominant kernel
   plan->ev_start = static_cast<cudaEvent_t>(ev_start);
   plan->ev_stop = static_cast<cudaEvent_t>(ev_stop);
   return BGEMM_SUCCESS;
@@ -997,6 +1146,7 @@ bgemm_status_t bgemm_plan_check_device(bgemm_plan_t plan, bgemm_stream_t stream)
   if (!plan) return set_error(BGEMM_ERROR_INVALID_VALUE, 1, -1, "plan is NULL");
   cudaError_t e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) return cuda_error(e, "cudaStreamSynchronize");
+  if (plan->mix_tc) plan = plan->mix_tc;
   if (plan->mode == BGEMM_MODE_SIMT_FP32) return BGEMM_SUCCESS;
   return tc_check_device(plan, stream);
 }

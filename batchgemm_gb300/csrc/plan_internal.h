@@ -81,6 +81,11 @@ struct bgemm_plan_s {
   std::vector<bgemm::MatDesc> host_descs;
   bgemm_plan_info_t info{};
   unsigned long long* d_cta_times = nullptr;  // profiling hook: per-CTA start/end times
+  // Mixed plan (options.simt_below > 0): two child plans over masked sizes --
+  // matrices with min(M, N, K) < simt_below on FP32 SIMT, the rest in the
+  // plan's tensor-core mode; both take the caller's full pointer arrays.
+  bgemm_plan_s* mix_simt = nullptr;
+  bgemm_plan_s* mix_tc = nullptr;
   cudaEvent_t ev_start = nullptr;  // profiling hook around the GEMM launch
   cudaEvent_t ev_stop = nullptr;
 };

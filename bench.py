@@ -233,9 +233,9 @@ def gpu_leg(args, rank, world, local):
         s.synchronize()
         return fp64_sampled_error(db, C0=C0, beta=w.beta, alpha=w.alpha)
 
-    def time_mode(mode, steps, warmup, sample_clocks=False):
+    def time_mode(mode, steps, warmup, sample_clocks=False, **plan_kw):
         with torch.cuda.stream(s):
-            plan = db.plan(mode, stream=s)
+            plan = db.plan(mode, stream=s, **plan_kw)
         info = plan.info()
         # warm-up outside the graph, then capture one step
         for _ in range(max(1, min(warmup, 2))):
@@ -351,6 +351,18 @@ def gpu_leg(args, rank, world, local):
                 p2.close()
             except bg.BgemmError as e:
                 extra[mode] = {"unavailable": e.message}
+        # mixed plan: matrices with min(M, N, K) < 64 on the FP32 SIMT kernel,
+        # the rest in 3xTF32 (two GEMM kernels per execute)
+        try:
+            p2, inf2, ms2, _ = time_mode("tf32x3", max(3, args.steps // 4), 3, simt_below=64)
+            e2 = one_step_error(p2)
+            extra["tf32x3_mixed_simt_below_64"] = {
+                "tflops": round(flops / (ms2 * 1e-3) / 1e12, 3), "ms_per_step": round(ms2, 4),
+                "err_vs_fp64_max": e2[0], "err_vs_fp64_mean": e2[1],
+                "kernels_per_execute": inf2["kernels_per_execute"]}
+            p2.close()
+        except bg.BgemmError as e:
+            extra["tf32x3_mixed_simt_below_64"] = {"unavailable": e.message}
         # the same batch through the device-size entry (sizes and pointers in
         # device arrays, tile queue / workspace / tensor maps built on the
         # device; C += A B, so C is read as well), one captured call per step
@@ -568,8 +580,10 @@ def stream_leg(args, dev, s):
         arrs.append(tuple(bg.int_array(v) for v in (w.M, w.N, w.K, lda, ldb, lda)))
     flops = [w.flops() for w in bs]
 
-    def run(mode):
+    def run(mode, simt_below=0):
         opts = {"kernel_family": "pair"} if mode in ("tf32x3", "bf16x3") else {}
+        if simt_below:
+            opts["simt_below"] = simt_below
         t0 = time.perf_counter()
         reqs = [bg.plan_requirements(*arrs[b], mode=mode, **opts) for b in range(nb)]
         req_ms = (time.perf_counter() - t0) * 1e3 / nb
@@ -738,6 +752,13 @@ def stream_leg(args, dev, s):
         except bg.BgemmError as e:
             out[mode] = {"unavailable": e.message}
         torch.cuda.empty_cache()
+        if mode != "simt":
+            # mixed plan: min(M, N, K) < 64 on FP32 SIMT, the rest on tensor cores
+            try:
+                out[mode + "_mixed_simt_below_64"] = run(mode, simt_below=64)
+            except bg.BgemmError as e:
+                out[mode + "_mixed_simt_below_64"] = {"unavailable": e.message}
+        torch.cuda.empty_cache()
         try:
             out["device_sizes_" + mode] = run_device_sizes(mode)
         except bg.BgemmError as e:
@@ -749,6 +770,9 @@ def stream_leg(args, dev, s):
         a, b = out.get("device_sizes_" + args.mode, {}), out.get("device_sizes_simt", {})
         if "tflops" in a and "tflops" in b:
             out["ratio_vs_simt_device_sizes"] = round(a["tflops"] / b["tflops"], 3)
+        m = out.get(args.mode + "_mixed_simt_below_64", {})
+        if "tflops" in m:
+            out["ratio_vs_simt_mixed"] = round(m["tflops"] / out["simt"]["tflops"], 3)
     for key in list(pools):
         del pools[key]
     return out

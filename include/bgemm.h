@@ -104,7 +104,9 @@ typedef struct bgemm_plan_requirements {
   int pack_jobs;           /* split/pack pre-pass jobs (tensor-core modes)   */
   int kernel_family;       /* 0 SIMT, 1 one-SM tcgen05 tiles, 2 CTA-pair tiles */
   size_t workspace_bytes;  /* split-operand workspace (tensor-core modes)    */
-  int reserved[4];
+  int simt_tiles;          /* mixed plans (options.simt_below): tiles of the
+                              matrices that run on the FP32 SIMT kernel      */
+  int reserved[3];
 } bgemm_plan_requirements_t;
 
 /* Options for bgemm_plan_create_ex (zero-initialise, then set fields). */
@@ -119,7 +121,18 @@ typedef struct bgemm_plan_options {
   int layout;               /* bgemm_layout_t of every matrix (0: column-major) */
   int trans_a;              /* bgemm_op_t applied to every A (0: N)          */
   int trans_b;              /* bgemm_op_t applied to every B (0: N)          */
-  int reserved[3];          /* must be zero                                  */
+  int simt_below;           /* tensor-core modes: matrices with min(M, N, K)
+                               below this run on the FP32 SIMT kernel in the
+                               same execute, the rest on the tensor cores
+                               (0: all on the tensor cores).  Thin and short
+                               matrices are memory-bound, and the SIMT kernel
+                               reads 4 B per operand element where the split
+                               path moves ~20 B; their results are the FP32
+                               chain's, so the batch's error cannot exceed
+                               the all-SIMT path's where the tensor-core
+                               matrices beat it.  Two GEMM kernels per execute
+                               instead of one. */
+  int reserved[2];          /* must be zero                                  */
   /* Capacity for bgemm_plan_update: each field is raised to the creating
    * batch's own requirement, so all-zero means "this batch only".
    * kernel_family is ignored here (see the field above). */
