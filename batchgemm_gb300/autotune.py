@@ -44,7 +44,8 @@ import numpy as np
 PKG = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(PKG))
 
-SIMT_CFGS = [(16, 16), (32, 32), (64, 32), (32, 64), (64, 64), (128, 64), (64, 128), (128, 128)]
+SIMT_CFGS = [(16, 16), (32, 32), (64, 32), (32, 64), (64, 64), (128, 64), (64, 128), (128, 128),
+             (8, 128), (128, 8)]
 MODE_IDS = {"tf32": 1, "tf32x3": 2, "bf16x3": 3}
 
 
@@ -210,7 +211,7 @@ def current_tables():
     L = bg.lib()
     a, b = ctypes.c_float(), ctypes.c_float()
     simt = []
-    for c in range(8):
+    for c in range(len(SIMT_CFGS)):
         L.bgemm_debug_tile_cost(0, c, ctypes.byref(a), ctypes.byref(b))
         simt.append((a.value, b.value))
     tc = {}
@@ -235,7 +236,7 @@ def write_table(out, simt, tc, sched, dev_name, num_sms):
         "// Generated by batchgemm_gb300/autotune.py on %s (%s, %d SMs); do not edit." % (
             datetime.date.today().isoformat(), dev_name, num_sms),
         "// Per-tile time t = a + b*K in ns, measured with every persistent CTA busy.",
-        "constexpr TileCost kSimtCost[8] = {%s};" % ", ".join(row(v) for v in simt),
+        "constexpr TileCost kSimtCost[%d] = {%s};" % (len(simt), ", ".join(row(v) for v in simt)),
         "constexpr TileCost kTcCost[3][16] = {\n%s};" % ",\n".join(
             "  {%s}" % ", ".join(row(v) for v in tc[m]) for m in ("tf32", "tf32x3", "bf16x3")),
         "// Promotion groups of the split modes on CTA pairs per bucket of K (128-byte",
@@ -286,7 +287,8 @@ def main():
     tc = {m: list(v) for m, v in tc_cur.items()}
     for mode in args.modes.split(","):
         Ks = [16, 64, 256, 1024] if mode == "simt" else [32, 128, 512, 2048]
-        cfgs = range(8) if mode == "simt" else [c for c in range(16) if valid_tc(mode, c)]
+        cfgs = range(len(SIMT_CFGS)) if mode == "simt" else [c for c in range(16)
+                                                               if valid_tc(mode, c)]
         for c in cfgs:
             slots = simt_slots if mode == "simt" else (tc_slots // 2 if c >= 8 else tc_slots)
             ts = []

@@ -48,10 +48,14 @@ struct TileItem {
 struct SimtCfg {
   int bm, bn, tm, tn;
 };
-constexpr int kSimtNumCfgs = 8;
+// Ids 8 and 9 are the thin tiles: 8 x 128 for M <= 8 (each thread four rows
+// of one column) and 128 x 8 for N <= 8 (one row of four columns), where the
+// 16-wide tiles would compute mostly padding.
+constexpr int kSimtNumCfgs = 10;
 constexpr SimtCfg kSimtCfgs[kSimtNumCfgs] = {
     {16, 16, 1, 1},  {32, 32, 2, 2},  {64, 32, 4, 2},  {32, 64, 2, 4},
     {64, 64, 4, 4},  {128, 64, 8, 4}, {64, 128, 4, 8}, {128, 128, 8, 8},
+    {8, 128, 4, 1},  {128, 8, 1, 4},
 };
 
 struct SimtParams {

@@ -60,6 +60,11 @@ __host__ __device__ inline long long fw_tiles(int M, int N, const SimtCfg& g) {
 __host__ __device__ inline float fw_tile_ns(int K, const TileCost& c) {
   return fmaf(c.b_ns, (float)K, c.a_ns);
 }
+// TileItem holds 16-bit tile coordinates: a configuration with more than
+// 65535 tiles along M or N is not a candidate (the host planner's rule).
+__host__ __device__ inline bool fw_fits(int M, int N, const SimtCfg& g) {
+  return (M + g.bm - 1) / g.bm <= 65535 && (N + g.bn - 1) / g.bn <= 65535;
+}
 __host__ __device__ inline long long fw_work(int M, int N, int K, int cfg, const SimtCfg* cfgs,
                                              const TileCost* cost) {
   return fw_tiles(M, N, cfgs[cfg]) * (long long)fw_tile_ns(K, cost[cfg]);
@@ -73,6 +78,7 @@ __host__ __device__ inline FwMat fw_plan_matrix(int M, int N, int K, int max_dim
   if (!r.bad && M > 0 && N > 0) {
     double bw = 0.0;
     for (int c = kSimtNumCfgs - 1; c >= 0; --c) {
+      if (!fw_fits(M, N, cfgs[c])) continue;
       const long long t = fw_tiles(M, N, cfgs[c]);
       const double w = (double)t * fw_tile_ns(K, cost[c]);
       if (r.cfg < 0 || w < bw * 0.999) {
@@ -103,6 +109,7 @@ __host__ __device__ inline int fw_rebalance(int M, int N, int K, int cfg, long l
   int best = -1;
   long long bw = 0, btt = 0;
   for (int c = 0; c < kSimtNumCfgs; ++c) {
+    if (!fw_fits(M, N, cfgs[c])) continue;
     const long long t2 = (long long)fw_tile_ns(K, cost[c]);
     const long long n2 = fw_tiles(M, N, cfgs[c]);
     if (t2 >= tt || n2 <= tiles) continue;

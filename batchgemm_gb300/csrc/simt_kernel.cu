@@ -396,6 +396,102 @@ __device__ __forceinline__ void simt_tile(const MatDesc& d, int tm, int tn,
   }
 }
 
+// Thin tiles.  THIN_M: an 8 x 128 tile (M <= 8), thread t owns column t % 128
+// and rows 4 (t / 128) .. +3; otherwise a 128 x 8 tile (N <= 8), thread t owns
+// row t % 128 and columns 4 (t / 128) .. +3.  Same cp.async ring of 16-k
+// slices and the same per-element fma chain over k in order as simt_tile, so
+// results are bit-identical to every other configuration.
+template <bool THIN_M, bool GEN = false>
+__device__ __forceinline__ void simt_thin(const MatDesc& d, int tm, int tn,
+                                          const float* __restrict__ A,
+                                          const float* __restrict__ B, float* __restrict__ C,
+                                          float alpha, float beta, float* smem) {
+  constexpr int BM = THIN_M ? 8 : 128;
+  constexpr int BN = THIN_M ? 128 : 8;
+  constexpr int LDAS = BM + kPadB;  // rows of k padded like the transposed loads
+  constexpr int LDBS = BN + kPadB;
+  constexpr int A_STAGE = kBK * LDAS;
+  constexpr int STAGE = A_STAGE + kBK * LDBS;
+  static_assert(kStages * STAGE <= kStages * kMaxStageFloats, "thin stage fits the ring");
+  const int tid = threadIdx.x;
+  const int M = d.M, N = d.N, K = d.K;
+  const long long lda = d.lda, ldb = d.ldb, ldc = d.ldc;
+  const int m0 = tm * BM, n0 = tn * BN;
+  const bool inplace = (alpha == 1.0f && beta == 1.0f);
+  // this thread's outputs: (m_of(r), n_of(r)) for r = 0..3
+  const int own = tid & 127, quad = tid >> 7;
+  auto m_of = [&](int r) { return THIN_M ? m0 + 4 * quad + r : m0 + own; };
+  auto n_of = [&](int r) { return THIN_M ? n0 + own : n0 + 4 * quad + r; };
+
+  const bool ta = GEN && (d.aux & kTransAFlag), tb = GEN && (d.aux & kTransBFlag);
+  const bool a_vec = !ta && ((reinterpret_cast<uintptr_t>(A) & 15u) == 0) && ((d.lda & 3) == 0);
+  const bool b_vec = tb && ((reinterpret_cast<uintptr_t>(B) & 15u) == 0) && ((d.ldb & 3) == 0);
+  auto load_stage = [&](int kb, int slot) {
+    float* sA = smem + slot * STAGE;
+    float* sB = sA + A_STAGE;
+    const int k0 = kb * kBK;
+    if (!ta)
+      load_rows_contig<BM, LDAS>(A, lda, M, m0, k0, K, sA, a_vec, tid);
+    else
+      load_k_contig<BM, LDAS>(A, lda, M, m0, k0, K, sA, tid);
+    if (tb)
+      load_rows_contig<BN, LDBS>(B, ldb, N, n0, k0, K, sB, b_vec, tid);
+    else
+      load_k_contig<BN, LDBS>(B, ldb, N, n0, k0, K, sB, tid);
+  };
+  const int nkb = (K + kBK - 1) / kBK;
+#pragma unroll
+  for (int s = 0; s < kStages - 1; ++s) {
+    if (s < nkb) load_stage(s, s);
+    cp_async_commit();
+  }
+  float acc[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    float v = 0.0f;
+    if (inplace && m_of(r) < M && n_of(r) < N) v = C[(long long)n_of(r) * ldc + m_of(r)];
+    acc[r] = v;
+  }
+  for (int kb = 0; kb < nkb; ++kb) {
+    cp_async_wait<kStages - 2>();
+    __syncthreads();
+    {
+      const int nk = kb + kStages - 1;
+      if (nk < nkb) load_stage(nk, nk % kStages);
+      cp_async_commit();
+    }
+    const float* sA = smem + (kb % kStages) * STAGE;
+    const float* sB = sA + A_STAGE;
+#pragma unroll
+    for (int k = 0; k < kBK; ++k) {
+      if constexpr (THIN_M) {
+        const float b = sB[k * LDBS + own];
+        const float4 a = *reinterpret_cast<const float4*>(sA + k * LDAS + 4 * quad);
+        acc[0] = fmaf(a.x, b, acc[0]);
+        acc[1] = fmaf(a.y, b, acc[1]);
+        acc[2] = fmaf(a.z, b, acc[2]);
+        acc[3] = fmaf(a.w, b, acc[3]);
+      } else {
+        const float a = sA[k * LDAS + own];
+        const float4 b = *reinterpret_cast<const float4*>(sB + k * LDBS + 4 * quad);
+        acc[0] = fmaf(a, b.x, acc[0]);
+        acc[1] = fmaf(a, b.y, acc[1]);
+        acc[2] = fmaf(a, b.z, acc[2]);
+        acc[3] = fmaf(a, b.w, acc[3]);
+      }
+    }
+  }
+  cp_async_wait<0>();
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int m = m_of(r), n = n_of(r);
+    if (m < M && n < N) {
+      float* p = C + (long long)n * ldc + m;
+      *p = inplace ? acc[r] : (beta == 0.0f ? alpha * acc[r] : fmaf(alpha, acc[r], beta * *p));
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 2) simt_persistent_kernel(const SimtParams p) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_item;
@@ -418,7 +514,9 @@ __global__ void __launch_bounds__(kThreads, 2) simt_persistent_kernel(const Simt
       case 4: simt_tile<64, 64, 4, 4>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
       case 5: simt_tile<128, 64, 8, 4>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
       case 6: simt_tile<64, 128, 4, 8>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
-      default: simt_tile<128, 128, 8, 8>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 7: simt_tile<128, 128, 8, 8>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 8: simt_thin<true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      default: simt_thin<false>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
     }
     __syncthreads();
   }
@@ -459,7 +557,9 @@ __global__ void __launch_bounds__(kThreads, 2) simt_persistent_kernel_t(const Si
       case 4: simt_tile<64, 64, 4, 4, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
       case 5: simt_tile<128, 64, 8, 4, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
       case 6: simt_tile<64, 128, 4, 8, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
-      default: simt_tile<128, 128, 8, 8, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 7: simt_tile<128, 128, 8, 8, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      case 8: simt_thin<true, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
+      default: simt_thin<false, true>(d, ti.tm, ti.tn, A, B, C, p.alpha, p.beta, smem); break;
     }
     __syncthreads();
   }

@@ -26,11 +26,12 @@ struct TileCost {
 #else
 // Defaults from a first-principles model.  SIMT: 2 CTAs per SM share 128
 // FP32 lanes at ~1.9 GHz, b = BM*BN / (64 lanes * 1.9 GHz) / efficiency.
-constexpr TileCost kSimtCost[8] = {
+constexpr TileCost kSimtCost[10] = {
     {1500.f, 16 * 16 / 64 / 1.9f / 0.20f},    {1600.f, 32 * 32 / 64 / 1.9f / 0.45f},
     {1700.f, 64 * 32 / 64 / 1.9f / 0.60f},    {1700.f, 32 * 64 / 64 / 1.9f / 0.60f},
     {1800.f, 64 * 64 / 64 / 1.9f / 0.70f},    {2000.f, 128 * 64 / 64 / 1.9f / 0.80f},
     {2000.f, 64 * 128 / 64 / 1.9f / 0.80f},   {2200.f, 128 * 128 / 64 / 1.9f / 0.85f},
+    {1600.f, 8 * 128 / 64 / 1.9f / 0.45f},    {1600.f, 128 * 8 / 64 / 1.9f / 0.45f},
 };
 // Tensor cores: per 128-byte K slice a tile streams its operands from L2,
 // which bounds the narrow tiles, so a tile costs at least what a 128-wide

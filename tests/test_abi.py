@@ -9,7 +9,8 @@ import pytest
 import batchgemm_gb300 as bg
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-SIMT_CFGS = [(16, 16), (32, 32), (64, 32), (32, 64), (64, 64), (128, 64), (64, 128), (128, 128)]
+SIMT_CFGS = [(16, 16), (32, 32), (64, 32), (32, 64), (64, 64), (128, 64), (64, 128), (128, 128),
+             (8, 128), (128, 8)]
 
 
 def declared_symbols():
@@ -176,7 +177,7 @@ def test_rebalance_splits_tiles_for_small_batches(built_lib):
 
 
 def test_forced_config(built_lib):
-    for c in range(8):
+    for c in range(len(SIMT_CFGS)):
         cfgs, items = simt_queue([100, 7], [90, 300], [5, 5], force=c)
         assert cfgs == [c, c]
         coverage_ok([100, 7], [90, 300], cfgs, items)

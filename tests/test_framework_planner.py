@@ -189,7 +189,8 @@ def test_device_planner_replay_prefers_pair_tiles_of_the_cost_table(built_lib):
 
 
 # ---- the SIMT entry (bgemm_framework_gemm) -------------------------------
-SIMT_CFGS = [(16, 16), (32, 32), (64, 32), (32, 64), (64, 64), (128, 64), (64, 128), (128, 128)]
+SIMT_CFGS = [(16, 16), (32, 32), (64, 32), (32, 64), (64, 64), (128, 64), (64, 128), (128, 128),
+             (8, 128), (128, 8)]
 
 
 SLOTS = 304  # persistent SIMT CTAs on GB300 (152 SMs x 2)

@@ -67,7 +67,7 @@ def test_zero_and_empty_matrices(cuda):
     run_case([4, 5], [6, 5], [0, 0], 1.0, 1.0)
 
 
-@pytest.mark.parametrize("cfg", range(8))
+@pytest.mark.parametrize("cfg", range(10))
 def test_every_tile_config(cuda, cfg):
     rng = np.random.default_rng(cfg)
     M = rng.integers(1, 300, 12).tolist()

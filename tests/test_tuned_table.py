@@ -60,7 +60,7 @@ def test_k_buckets():
 def test_cost_table_positive_for_every_runnable_configuration(built_lib):
     L = bg.lib()
     a, b = ctypes.c_float(), ctypes.c_float()
-    for c in range(8):
+    for c in range(10):
         assert L.bgemm_debug_tile_cost(0, c, ctypes.byref(a), ctypes.byref(b)) == 0
         assert a.value > 0 and b.value > 0
     for mode in (1, 2, 3):
