@@ -265,3 +265,24 @@ def test_simt_device_planner_rebalances_small_batches(built_lib):
     _, b, _ = fw_simt_plan(M, M, M, 1024)
     assert len(a) == len(b)  # thousands of tiles for 304 CTAs: nothing to rebalance
 
+
+
+def test_thin_matrices_take_thin_tiles_within_16_bit_coordinates(built_lib):
+    """M <= 8 (or N <= 8) matrices take the 8 x 128 (or 128 x 8) tiles; a
+    matrix whose thin-tile grid would pass 65535 tiles along a side takes a
+    configuration that fits the 16-bit tile coordinates, in both planners."""
+    from test_abi import simt_queue
+    M = [4, 2000, 8, 3000]
+    N = [2000, 4, 3000, 8]
+    K = [64, 64, 16, 16]
+    # one CTA slot: no rebalance for parallelism splits the tiles further
+    for cfgs, items in (fw_simt_plan(M, N, K, 4096, slots=1)[:2], simt_queue(M, N, K, slots=1)):
+        assert cfgs == [8, 9, 8, 9], cfgs
+    tall = [700000, 5]
+    wide = [3, 700000]
+    for cfgs, items in (fw_simt_plan(tall, wide, [2, 2], 1 << 20)[:2],
+                        simt_queue(tall, wide, [2, 2])):
+        for i in range(2):
+            bm, bn = SIMT_CFGS[cfgs[i]]
+            assert -(-tall[i] // bm) <= 65535 and -(-wide[i] // bn) <= 65535, cfgs
+        assert items[:, 1].max() <= 65535 and items[:, 2].max() <= 65535
