@@ -31,7 +31,8 @@
 //             peer's TMA completes on the leader's barrier (cta_group::2 TMA);
 //   empty[s]  both CTAs: the leader's commit is multicast to the pair;
 //   tfull[b]  both CTAs: multicast commit when a group's MMAs finish;
-//   tempty[b] leader only: 16 arrivals (8 epilogue warps x 2 CTAs);
+//   tempty[b] leader only: 16 arrivals (8 epilogue warps x 2 CTAs), relaxed:
+//             each warp's TMEM loads have completed before it arrives;
 //   sfull[j]  both CTAs: the leader's producer published schedule slot j;
 //   sempty[j] leader only: 18 arrivals (leader MMA lane, peer producer,
 //             8 epilogue warps x 2 CTAs) once slot j has been read.
@@ -491,7 +492,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
         }
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive_cluster(mapa_shared(tempty(acc.idx), 0));
+        if (lane == 0) mbar_arrive_cluster_relaxed(mapa_shared(tempty(acc.idx), 0));
         acc.next(kNAcc);
       }
       if (!ok) break;
