@@ -19,13 +19,24 @@ and maximum error are both no worse than FP32 SIMT's (3xBF16, whose split
 error is far above FP32's: the fastest within 2 % of its most accurate
 group's mean).
 
-Both results are written to ``csrc/tile_table_tuned.inc``, which the library
+Compile-time parameters (--build-params).  Two schedule constants are
+template arguments of the kernels: the SIMT kernel's cp.async ring cap (a
+small tile takes as many 16-k stages as the CTA's shared memory holds, up to
+the cap) and the CTA-pair kernel's C-prefetch lead for beta != 0.  For each
+candidate the table is rewritten, the library rebuilt, and a child process
+times the workloads the parameter affects (ring: configs 1 and 2 and eight
+stream batches on SIMT; lead: config 2 and eight stream batches in 3xTF32,
+both beta != 0); the candidate with the least geometric-mean time is kept,
+one parameter after the other.
+
+All results are written to ``csrc/tile_table_tuned.inc``, which the library
 compiles in place of the analytic defaults of ``csrc/tile_table.h``; what a
 run does not measure is copied from the library's current tables.
 
   python -m batchgemm_gb300.autotune                     # tile costs, print
   python -m batchgemm_gb300.autotune --write             # ... and write
   python -m batchgemm_gb300.autotune --schedule --write  # schedule, write
+  python -m batchgemm_gb300.autotune --build-params      # rebuild per candidate, write
 
 The split/pack pre-pass of the tensor-core modes does not depend on the tile
 configuration; its time is estimated from its bytes (read 4 B, write 4 or 8
@@ -36,7 +47,9 @@ from __future__ import annotations
 import argparse
 import datetime
 import json
+import math
 import os
+import subprocess
 import sys
 
 import numpy as np
@@ -226,10 +239,83 @@ def current_tables():
         g = (ctypes.c_int * 8)()
         L.bgemm_debug_get_tc_schedule(mid, g)
         sched[mode] = list(g)
-    return simt, tc, sched
+    ring, lead = ctypes.c_int(), ctypes.c_int()
+    L.bgemm_debug_build_params(ctypes.byref(ring), ctypes.byref(lead))
+    params = {"simt_ring_cap": ring.value, "c_prefetch_lead": lead.value}
+    return simt, tc, sched, params
 
 
-def write_table(out, simt, tc, sched, dev_name, num_sms):
+BUILD_CANDIDATES = {"simt_ring_cap": [4, 6, 8], "c_prefetch_lead": [1, 2, 3, 4]}
+
+
+def measure_build_params(which, reps=5):
+    """Child process: times (ms) of the workloads a compile-time parameter
+    affects, on the library as built."""
+    import torch
+    from batchgemm_gb300 import workloads
+    from batchgemm_gb300.batch import DeviceBatch
+
+    def timed(w, mode, alpha, beta):
+        db = DeviceBatch(w.M, w.N, w.K).fill_fast("uniform", 0)
+        with db.plan(mode) as p:
+            for _ in range(3):
+                db.execute(p, alpha, beta)
+            torch.cuda.synchronize()
+            ts = []
+            for _ in range(reps):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                db.execute(p, alpha, beta)
+                e1.record()
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            p.check_device()
+        del db
+        torch.cuda.empty_cache()
+        return float(np.median(ts))
+
+    stream = workloads.stream_batches(0, 8)
+    out = {}
+    if which == "simt_ring_cap":
+        out["plain_fp32_256"] = timed(workloads.plain_fp32(0), "simt", 1.0, 0.0)
+        out["simt_at_scale_2048"] = timed(workloads.simt_at_scale(0), "simt", 1.0, 0.5)
+        out["stream8"] = sum(timed(w, "simt", 1.0, 1.0) for w in stream)
+    else:
+        out["simt_at_scale_2048"] = timed(workloads.simt_at_scale(0), "tf32x3", 1.0, 0.5)
+        out["stream8"] = sum(timed(w, "tf32x3", 1.0, 1.0) for w in stream)
+    return out
+
+
+def sweep_build_params(args, tables, dev_name, num_sms):
+    """Rebuild per candidate and keep the fastest value of each parameter."""
+    simt, tc, sched, params = tables
+    params = dict(params)
+    root = os.path.dirname(PKG)
+    result = {}
+    for name, cands in BUILD_CANDIDATES.items():
+        res = {}
+        for v in cands:
+            trial = dict(params, **{name: v})
+            write_table(args.out, simt, tc, sched, dev_name, num_sms, trial)
+            subprocess.check_call([sys.executable, "-c", "import batchgemm_gb300 as bg; bg.build()"],
+                                  cwd=root, stdout=subprocess.DEVNULL)
+            txt = subprocess.check_output([sys.executable, "-m", "batchgemm_gb300.autotune",
+                                           "--measure-build-params", name], cwd=root)
+            res[v] = json.loads(txt.decode().strip().splitlines()[-1])
+            print("build param %s = %d: %s" % (name, v, json.dumps(res[v])), flush=True)
+        # least geometric-mean time over the workloads
+        score = {v: sum(math.log(t) for t in r.values()) for v, r in res.items()}
+        params[name] = min(score, key=score.get)
+        result[name] = {"times_ms": {str(v): r for v, r in res.items()}, "pick": params[name]}
+        print("build param %s -> %d" % (name, params[name]), flush=True)
+    write_table(args.out, simt, tc, sched, dev_name, num_sms, params)
+    subprocess.check_call([sys.executable, "-c", "import batchgemm_gb300 as bg; bg.build()"],
+                          cwd=root, stdout=subprocess.DEVNULL)
+    return result
+
+
+def write_table(out, simt, tc, sched, dev_name, num_sms, params):
     def row(v):
         return "{%.1ff, %.4ff}" % tuple(v) if v else "{0.f, 0.f}"
     lines = [
@@ -245,6 +331,10 @@ def write_table(out, simt, tc, sched, dev_name, num_sms):
         "constexpr unsigned char kTcGroupTable[3][8] = {%s};" % ", ".join(
             "{%s}" % ", ".join(str(int(x)) for x in sched[m]) for m in ("tf32", "tf32x3",
                                                                         "bf16x3")),
+        "// Compile-time schedule parameters: SIMT ring cap, pair-kernel C-prefetch lead.",
+        "#define BGEMM_TUNED_HAS_BUILD_PARAMS 1",
+        "constexpr int kSimtRingCap = %d;" % int(params["simt_ring_cap"]),
+        "constexpr int kTcCPrefetchLead = %d;" % int(params["c_prefetch_lead"]),
     ]
     with open(out, "w") as f:
         f.write("\n".join(lines) + "\n")
@@ -259,12 +349,24 @@ def main():
     ap.add_argument("--schedule", action="store_true",
                     help="sweep the promotion schedule instead of the tile costs")
     ap.add_argument("--json", default=None, help="also dump raw measurements here")
+    ap.add_argument("--build-params", action="store_true",
+                    help="sweep the compile-time parameters (rebuilds the library), write")
+    ap.add_argument("--measure-build-params", default=None, help=argparse.SUPPRESS)
     args = ap.parse_args()
     import torch
     import batchgemm_gb300 as bg
     bg.lib()
+    if args.measure_build_params:
+        print(json.dumps(measure_build_params(args.measure_build_params)), flush=True)
+        return
     dev = bg.device_info()
-    simt_cur, tc_cur, sched_cur = current_tables()
+    simt_cur, tc_cur, sched_cur, params_cur = current_tables()
+    if args.build_params:
+        res = sweep_build_params(args, (simt_cur, tc_cur, sched_cur, params_cur),
+                                 torch.cuda.get_device_name(0), dev["num_sms"])
+        if args.json:
+            json.dump(res, open(args.json, "w"), indent=1)
+        return
     if args.schedule:
         modes = [m for m in args.modes.split(",") if m in ("tf32x3", "bf16x3")]
         sched = dict(sched_cur)
@@ -273,7 +375,7 @@ def main():
             json.dump(sched, open(args.json, "w"), indent=1)
         if args.write:
             write_table(args.out, simt_cur, tc_cur, sched, torch.cuda.get_device_name(0),
-                        dev["num_sms"])
+                        dev["num_sms"], params_cur)
         return
     peaks = {}
     pk = os.path.join(os.path.dirname(PKG), "MEASURED_PEAKS.json")
@@ -307,7 +409,7 @@ def main():
         json.dump(raw, open(args.json, "w"), indent=1)
     if args.write:
         write_table(args.out, simt, tc, sched_cur, torch.cuda.get_device_name(0),
-                    dev["num_sms"])
+                    dev["num_sms"], params_cur)
 
 
 if __name__ == "__main__":

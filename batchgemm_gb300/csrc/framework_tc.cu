@@ -510,6 +510,14 @@ extern "C" int bgemm_debug_framework_tc_plan(const int* M, const int* N, const i
   return n_items;
 }
 
+// The compile-time schedule parameters of tile_table.h as built.
+extern "C" int bgemm_debug_build_params(int* simt_ring_cap, int* c_prefetch_lead) {
+  if (!simt_ring_cap || !c_prefetch_lead) return -1;
+  *simt_ring_cap = kSimtRingCap;
+  *c_prefetch_lead = kTcCPrefetchLead;
+  return 0;
+}
+
 // The cost-model entry (a + b*K ns per tile) the planners use for a mode's
 // configuration: the SIMT table (mode 0) or the tensor-core table as the
 // device planner completes it.

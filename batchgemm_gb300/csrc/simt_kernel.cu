@@ -9,7 +9,8 @@
 //
 // Each item is one BM x BN output tile of one matrix.  256 threads form a
 // 16 x 16 grid; each owns a TM x TN register tile.  Operands stream through a
-// 4-stage cp.async ring of BK = 16 k-slices:
+// cp.async ring of BK = 16 k-slices (4 stages for 128 x 128 tiles, up to the
+// autotuned kSimtRingCap for smaller ones):
 //   A slice: [k][BM]     (column of A, 16-byte cp.async when lda % 4 == 0 and
 //                         A is 16-byte aligned, 4-byte otherwise)
 //   B slice: [k][BN + 4] (transposed on the way in by 4-byte cp.async; the
@@ -27,17 +28,28 @@
 #include <stdint.h>
 
 #include "bgemm_internal.h"
+#include "tile_table.h"
 
 namespace bgemm {
 namespace {
 
 constexpr int kThreads = 256;
 constexpr int kBK = 16;
-constexpr int kStages = 4;
+constexpr int kStages = 4;  // ring stages of the largest (128 x 128) tile
 constexpr int kPadB = 4;
 constexpr int kMaxStageFloats = kBK * (128 + 128 + kPadB);
 constexpr int kSmemBytes = kStages * kMaxStageFloats * 4;
 constexpr int kSmemBytesT = kStages * kBK * (128 + kPadB + 128 + kPadB) * 4;  // transposed kernel
+static_assert(kSimtRingCap >= kStages && kSimtRingCap <= 32, "SIMT ring cap out of range");
+
+// Stages of the cp.async ring for a tile whose stage holds `stage` floats: as
+// many as the kernel's shared memory holds, at most kSimtRingCap (autotuned).
+template <bool GEN>
+__host__ __device__ constexpr int ring_stages(int stage) {
+  return ((GEN ? kSmemBytesT : kSmemBytes) / 4 / stage) < kSimtRingCap
+             ? (GEN ? kSmemBytesT : kSmemBytes) / 4 / stage
+             : kSimtRingCap;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -251,21 +263,23 @@ __device__ __forceinline__ void simt_tile(const MatDesc& d, int tm, int tn,
     }
   };
 
+  constexpr int NS = ring_stages<GEN>(STAGE);
+  static_assert(NS >= kStages, "ring of at least kStages stages");
 #pragma unroll
-  for (int s = 0; s < kStages - 1; ++s) {
+  for (int s = 0; s < NS - 1; ++s) {
     if (s < nkb) load_stage(s, s);
     cp_async_commit();
   }
 
   for (int kb = 0; kb < nkb; ++kb) {
-    cp_async_wait<kStages - 2>();
+    cp_async_wait<NS - 2>();
     __syncthreads();
     {
-      const int nk = kb + kStages - 1;
-      if (nk < nkb) load_stage(nk, nk % kStages);
+      const int nk = kb + NS - 1;
+      if (nk < nkb) load_stage(nk, nk % NS);
       cp_async_commit();
     }
-    const float* sA = smem + (kb % kStages) * STAGE;
+    const float* sA = smem + (kb % NS) * STAGE;
     const float* sB = sA + A_STAGE;
 #pragma unroll
     for (int k = 0; k < kBK; ++k) {
@@ -412,7 +426,8 @@ __device__ __forceinline__ void simt_thin(const MatDesc& d, int tm, int tn,
   constexpr int LDBS = BN + kPadB;
   constexpr int A_STAGE = kBK * LDAS;
   constexpr int STAGE = A_STAGE + kBK * LDBS;
-  static_assert(kStages * STAGE <= kStages * kMaxStageFloats, "thin stage fits the ring");
+  constexpr int NS = ring_stages<GEN>(STAGE);
+  static_assert(NS >= kStages, "ring of at least kStages stages");
   const int tid = threadIdx.x;
   const int M = d.M, N = d.N, K = d.K;
   const long long lda = d.lda, ldb = d.ldb, ldc = d.ldc;
@@ -441,7 +456,7 @@ __device__ __forceinline__ void simt_thin(const MatDesc& d, int tm, int tn,
   };
   const int nkb = (K + kBK - 1) / kBK;
 #pragma unroll
-  for (int s = 0; s < kStages - 1; ++s) {
+  for (int s = 0; s < NS - 1; ++s) {
     if (s < nkb) load_stage(s, s);
     cp_async_commit();
   }
@@ -453,14 +468,14 @@ __device__ __forceinline__ void simt_thin(const MatDesc& d, int tm, int tn,
     acc[r] = v;
   }
   for (int kb = 0; kb < nkb; ++kb) {
-    cp_async_wait<kStages - 2>();
+    cp_async_wait<NS - 2>();
     __syncthreads();
     {
-      const int nk = kb + kStages - 1;
-      if (nk < nkb) load_stage(nk, nk % kStages);
+      const int nk = kb + NS - 1;
+      if (nk < nkb) load_stage(nk, nk % NS);
       cp_async_commit();
     }
-    const float* sA = smem + (kb % kStages) * STAGE;
+    const float* sA = smem + (kb % NS) * STAGE;
     const float* sB = sA + A_STAGE;
 #pragma unroll
     for (int k = 0; k < kBK; ++k) {

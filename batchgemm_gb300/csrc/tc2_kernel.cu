@@ -41,6 +41,7 @@
 
 #include "tc_epilogue.h"
 #include "tc_ptx.h"
+#include "tile_table.h"
 
 namespace bgemm {
 namespace {
@@ -82,7 +83,9 @@ __device__ __forceinline__ int group_slices(const TcGemmParams& p, int K) {
   return p.sched.group(tc_sched_bucket(K));
 }
 // beta != 0: promotion groups before the tile's end at which C is prefetched
-constexpr int kCPrefetchLead = 2;
+// (autotuned, tile_table.h)
+constexpr int kCPrefetchLead = kTcCPrefetchLead;
+static_assert(kCPrefetchLead >= 0 && kCPrefetchLead <= 16, "C prefetch lead out of range");
 
 // MMA width of a tile along the B side: bn, or for the matrix's last tile
 // column its remaining width rounded up to 16 (the pair MMA's N step), so

@@ -70,4 +70,16 @@ constexpr unsigned char kTcGroupTable[3][8] = {
     {0, 2, 2, 2, 2, 2, 2, 2}, {0, 2, 2, 2, 2, 2, 2, 2}, {0, 2, 2, 2, 2, 2, 2, 2}};
 #endif
 
+// Compile-time schedule parameters, swept by the autotuner with a rebuild per
+// candidate:
+//   kSimtRingCap      cp.async ring stages of a SIMT tile: a tile takes as
+//                     many 16-k stages as the CTA's shared memory holds, up
+//                     to this cap (the 128 x 128 tile always has 4);
+//   kTcCPrefetchLead  beta != 0: promotion groups before the end of a pair
+//                     tile at which its C lines are prefetched into L2.
+#if !defined(BGEMM_TUNED_HAS_BUILD_PARAMS)
+constexpr int kSimtRingCap = 4;
+constexpr int kTcCPrefetchLead = 2;
+#endif
+
 }  // namespace bgemm

@@ -76,6 +76,13 @@ int bgemm_debug_framework_tc_plan(const int* M, const int* N, const int* K, int 
  * invalid mode or configuration. */
 int bgemm_debug_tile_cost(int mode, int cfg, float* a_ns, float* b_ns);
 
+/* The compile-time schedule parameters the library was built with (from the
+ * autotuned table): *simt_ring_cap = the most cp.async ring stages of a SIMT
+ * tile, *c_prefetch_lead = promotion groups before the end of a CTA-pair
+ * tile at which its C is prefetched when beta != 0.  Returns 0, or -1 for a
+ * NULL argument. */
+int bgemm_debug_build_params(int* simt_ring_cap, int* c_prefetch_lead);
+
 /* Tensor-core plans: waits for `stream`, encodes on the host the tensor maps
  * that the device built for the plan, and compares them byte by byte.
  * *n_maps receives the number of maps compared, *n_diff how many differ,

@@ -69,3 +69,19 @@ def test_cost_table_positive_for_every_runnable_configuration(built_lib):
             if c >= 8 and (c & 3) == 3:
                 continue  # no such CTA-pair tile
             assert a.value > 0 and b.value > 0, (mode, c)
+
+
+def test_build_params_in_table_and_library(built_lib):
+    """The compile-time schedule parameters the autotuner sweeps with a
+    rebuild per candidate: written in the table, compiled into the library,
+    and one of the candidates."""
+    L = bg.lib()
+    text = open(INC).read()
+    ring = int(re.search(r"kSimtRingCap = (\d+);", text).group(1))
+    lead = int(re.search(r"kTcCPrefetchLead = (\d+);", text).group(1))
+    r, c = ctypes.c_int(), ctypes.c_int()
+    assert L.bgemm_debug_build_params(ctypes.byref(r), ctypes.byref(c)) == 0
+    assert (r.value, c.value) == (ring, lead)
+    assert ring in autotune.BUILD_CANDIDATES["simt_ring_cap"]
+    assert lead in autotune.BUILD_CANDIDATES["c_prefetch_lead"]
+    assert L.bgemm_debug_build_params(None, ctypes.byref(c)) == -1
