@@ -179,6 +179,7 @@ def lib() -> ctypes.CDLL:
     L.bgemm_debug_get_tc_schedule.argtypes = [i, vp]
     L.bgemm_debug_tile_cost.argtypes = [i, i, ctypes.POINTER(f), ctypes.POINTER(f)]
     L.bgemm_debug_build_params.argtypes = [ctypes.POINTER(i), ctypes.POINTER(i)]
+    L.bgemm_debug_hbm_probe.argtypes = [i, vp, vp, vp, ctypes.c_longlong, i, vp]
     for name in ("bgemm_sgemm_vbatched", "bgemm_plan_create", "bgemm_plan_create_ex",
                  "bgemm_plan_execute", "bgemm_plan_info", "bgemm_plan_check_device",
                  "bgemm_plan_destroy", "bgemm_framework_gemm", "bgemm_framework_check_device",

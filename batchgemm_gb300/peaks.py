@@ -13,7 +13,11 @@ Prints one JSON line with
   * ``own_tf32_pair_tflops``: this library's single-product TF32 mode on
     --cubes matrices of 1024^3 (CTA-pair tiles), GEMM kernel alone (CUDA
     events the library records around its launch), best of 10;
-  * the SM clocks sampled by nvidia-smi during the sustained loop.
+  * the SM clocks sampled by nvidia-smi during the sustained loop;
+  * ``hbm_mix_gbs``: HBM ceilings of four read:write mixes (one read and two
+    writes -- the split pre-pass's mix --, copy, write only, read only) from
+    the library's float4 streaming probe over 2 GiB buffers, best of two grid
+    sizes and 5 launches each.
 
 bench.py runs :func:`tf32_burst` itself on the box it measures on.
 """
@@ -63,6 +67,45 @@ def tf32_burst(reps=10):
         return rate
     finally:
         torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+HBM_KINDS = {0: ("read1_write2", 3), 1: ("copy", 2), 2: ("write_only", 1), 3: ("read_only", 1)}
+
+
+def hbm_mix(kinds=(0, 1, 2, 3), gib=2.0, reps=5):
+    """GB/s of the library's streaming probe (bgemm_debug_hbm_probe) per
+    read:write mix: algorithmic bytes over the best CUDA-event time."""
+    import torch
+    import batchgemm_gb300 as bg
+    L = bg.lib()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    n = int(gib * (1 << 30)) // 16 * 4  # floats, a whole number of float4 words
+    x = torch.rand(n, device="cuda")
+    y1 = torch.empty_like(x)
+    y2 = torch.empty_like(x)
+    st = torch.cuda.current_stream().cuda_stream
+    out = {}
+    try:
+        for kind in kinds:
+            name, words = HBM_KINDS[kind]
+            best = float("inf")
+            for grid in (8 * sms, 32 * sms):
+                for r in range(reps + 2):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    if L.bgemm_debug_hbm_probe(kind, x.data_ptr(), y1.data_ptr(), y2.data_ptr(),
+                                               n // 4, grid, st) != 0:
+                        raise RuntimeError("bgemm_debug_hbm_probe failed")
+                    e1.record()
+                    e1.synchronize()
+                    if r >= 2:
+                        best = min(best, e0.elapsed_time(e1))
+            out[name] = round(words * n * 4 / (best * 1e-3) / 1e9, 1)
+    finally:
+        del x, y1, y2
+        torch.cuda.empty_cache()
+    return out
 
 
 def _sustained(seconds):
@@ -164,6 +207,7 @@ def main() -> None:
         out["sustained_clocks"] = {"sm_mhz_median": statistics.median(busy),
                                    "sm_max_mhz": max(smax), "power_w_max": max(pw),
                                    "samples": len(sm)}
+    out["hbm_mix_gbs"] = hbm_mix()
     rate, ms, hist = own_tf32_pair(a.cubes)
     out["own_tf32_pair_tflops"] = round(rate, 1)
     out["own_tf32_pair"] = {"workload": "%d matrices 1024^3, TF32 mode, CTA-pair tiles" % a.cubes,

@@ -293,6 +293,13 @@ def gpu_leg(args, rank, world, local):
         from batchgemm_gb300 import peaks as peaks_mod
         out["tf32_peak"] = peaks_mod.tf32_burst()
         torch.cuda.empty_cache()
+    if args.mode in ("tf32", "tf32x3", "bf16x3"):
+        # the HBM ceiling of the pre-pass's read:write mix (3xTF32: read 4 B,
+        # write 8 B per element; TF32 and 3xBF16: read 4, write 4)
+        from batchgemm_gb300 import peaks as peaks_mod
+        out["pre_pass_mix"] = "read1_write2" if args.mode == "tf32x3" else "copy"
+        out["pre_pass_peak"] = peaks_mod.hbm_mix(kinds=(0 if args.mode == "tf32x3" else 1,),
+                                                 gib=1.0)[out["pre_pass_mix"]]
     plan, info, ms, clocks = time_mode(args.mode, args.steps, args.warmup, sample_clocks=True)
     value, ms_max = whole_job_tflops(flops, ms, world, dev)
     err_max, err_mean, nsamp = one_step_error(plan)
@@ -449,6 +456,16 @@ def gpu_leg(args, rank, world, local):
                            "step_dram_bytes": (traffic + pre_traffic
                                                if traffic and pre_traffic else None),
                            "pre_pass_traffic": pre_traffic}
+        elems = float(sum(m * k + k * n for m, n, k in zip(w.M, w.N, w.K)))
+        pre_bytes = elems * (4 + {"tf32": 4, "tf32x3": 8, "bf16x3": 4}[mode])
+        pre_ach = pre_bytes / (pre_ms * 1e-3) / 1e9
+        out["roofline"]["pre_pass"] = {
+            "bound": "hbm", "achieved": round(pre_ach, 1), "peak": out["pre_pass_peak"],
+            "unit": "GB/s", "frac": round(pre_ach / out["pre_pass_peak"], 4),
+            "algorithmic_bytes": pre_bytes,
+            "peak_source": "measured in this run before the timed region: the library's float4 "
+                           "streaming probe (bgemm_debug_hbm_probe) with the pre-pass's mix (%s), "
+                           "1 GiB buffers, best of two grids" % out["pre_pass_mix"]}
         if mode != "bf16x3" and "bf16_tflops" in peaks:
             out["roofline"]["bf16_measured_tflops"] = peaks["bf16_tflops"]
         if "cta_balance" in out:

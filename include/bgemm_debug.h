@@ -83,6 +83,16 @@ int bgemm_debug_tile_cost(int mode, int cfg, float* a_ns, float* b_ns);
  * NULL argument. */
 int bgemm_debug_build_params(int* simt_ring_cap, int* c_prefetch_lead);
 
+/* HBM streaming probe (no counterpart in the reference): launches one
+ * grid-stride float4 kernel of `grid` CTAs x 256 threads on `stream` over n4
+ * float4 words per buffer.  kind 0 reads x and writes y1 and y2 (one read,
+ * two writes: the split pre-pass's mix), 1 copies x to y1, 2 writes y1,
+ * 3 reads x (y1 is a sink).  The caller times it; batchgemm_gb300.peaks
+ * reports the ceilings.  Returns 0, or -1 for invalid arguments (a NULL or
+ * non-16-byte-aligned buffer the kind needs) or a failed launch. */
+int bgemm_debug_hbm_probe(int kind, const float* x, float* y1, float* y2, long long n4, int grid,
+                          void* stream);
+
 /* Tensor-core plans: waits for `stream`, encodes on the host the tensor maps
  * that the device built for the plan, and compares them byte by byte.
  * *n_maps receives the number of maps compared, *n_diff how many differ,
