@@ -24,9 +24,10 @@ template arguments of the kernels: the SIMT kernel's cp.async ring cap (a
 small tile takes as many 16-k stages as the CTA's shared memory holds, up to
 the cap) and the CTA-pair kernel's C-prefetch lead for beta != 0.  For each
 candidate the table is rewritten, the library rebuilt, and a child process
-times the workloads the parameter affects (ring: configs 1 and 2 and eight
-stream batches on SIMT; lead: config 2 and eight stream batches in 3xTF32,
-both beta != 0); the candidate with the least geometric-mean time is kept,
+times the workloads the parameter affects (ring: the plain 256-matrix batch,
+the 2048-matrix log-uniform batch and eight stream batches on SIMT; lead: the
+2048-matrix batch and eight stream batches in 3xTF32, both beta != 0); the
+candidate with the least geometric-mean time is kept,
 one parameter after the other.
 
 All results are written to ``csrc/tile_table_tuned.inc``, which the library

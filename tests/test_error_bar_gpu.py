@@ -53,7 +53,7 @@ def check_bound(mode, e, K, what):
         what, mode, bad.size, e[bad[0]], K[bad[0]], lim[bad[0]])
 
 
-def test_north_star_error_bar_skewed(cuda):
+def test_tf32x3_error_not_above_fp32_simt_skewed(cuda):
     """3xTF32 mean AND max error on the skewed batch <= FP32 SIMT's, same samples."""
     w = workloads.skewed(0)
     db = DeviceBatch(w.M, w.N, w.K).fill_fast(w.dist, seed=2)
@@ -72,7 +72,9 @@ def test_north_star_error_bar_skewed(cuda):
 
 @pytest.mark.parametrize("name", ["plain_fp32_256", "simt_at_scale_2048", "uneven_m_128"])
 def test_config_error_bounds(cuda, name):
-    """Configs 1, 2 and 4 whole, every mode within its bound on sampled entries."""
+    """The plain 256-matrix batch, the 2048-matrix log-uniform batch and the
+    uneven-M 128-matrix batch whole, every mode within its bound on sampled
+    entries."""
     w = workloads.CONFIGS[name](0)
     db = DeviceBatch(w.M, w.N, w.K).fill_fast(w.dist, seed=3)
     C0 = db.C.clone()

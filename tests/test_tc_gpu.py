@@ -240,7 +240,7 @@ def test_skewed_full_size_error_vs_fp64(cuda, mode):
     smax, smean, _ = bench.fp64_sampled_error(db, per_matrix=4, seed=1)
     print("%s: max %.3g mean %.3g | simt max %.3g mean %.3g" % (mode, emax, emean, smax, smean))
     # the strict comparison with FP32 SIMT (mean and max) is
-    # test_error_bar_gpu.py::test_north_star_error_bar_skewed
+    # test_error_bar_gpu.py::test_tf32x3_error_not_above_fp32_simt_skewed
 
 
 def test_bounded_wait_expires_and_context_survives(cuda):
