@@ -134,6 +134,26 @@ def test_framework_drop_in_golden_and_dataset(cuda):
         assert_bits_equal(db.C.cpu().numpy(), want, "framework dataset")
 
 
+def test_framework_thin_matrices_bit_exact(cuda):
+    """bgemm_framework_gemm on thin matrices (M <= 8 or N <= 8, long K), where
+    the device planner can choose the thin tiles: C += A*B stays bit-exact."""
+    rng = np.random.default_rng(17)
+    n = 24
+    thin = rng.integers(1, 9, n)
+    wide = rng.integers(200, 1500, n)
+    M = [int(t) if i % 2 == 0 else int(w) for i, (t, w) in enumerate(zip(thin, wide))]
+    N = [int(w) if i % 2 == 0 else int(t) for i, (t, w) in enumerate(zip(thin, wide))]
+    K = rng.integers(100, 700, n).tolist()
+    db, host = make_batch(M, N, K, seed=8)
+    want = oracle_batch(db, host, 1.0, 1.0)
+    dev = lambda v: torch.tensor(v, dtype=torch.int32, device="cuda")
+    dM, dN, dK = dev(M), dev(N), dev(K)
+    bg.framework_gemm(dM.data_ptr(), dN.data_ptr(), dK.data_ptr(), db.pA.data_ptr(),
+                      db.pB.data_ptr(), db.pC.data_ptr(), n, 2048)
+    bg.framework_check_device()
+    assert_bits_equal(db.C.cpu().numpy(), want, "framework thin")
+
+
 def test_framework_rejects_oversized_on_device(cuda):
     dev = lambda v: torch.tensor(v, dtype=torch.int32, device="cuda")
     from batchgemm_gb300.batch import DeviceBatch

@@ -175,3 +175,28 @@ def test_plan_with_layout_and_update(cuda, layout, ta, tb):
         torch.cuda.synchronize()
         p.check_device()
     c2.check_fp64(c2.result(), 1.0, 1.0, "tf32x3")
+
+
+@pytest.mark.parametrize("layout,ta,tb", COMBOS)
+def test_thin_tiles_bit_exact(cuda, layout, ta, tb):
+    """The thin SIMT tiles (8 x 128 for M <= 8, 128 x 8 for N <= 8), forced,
+    in every storage order and transposition: bit-exact with the oracle,
+    ragged edges and padding included."""
+    rng = np.random.default_rng(40 + COMBOS.index((layout, ta, tb)))
+    for cfg, thin in ((8, "M"), (9, "N")):
+        n = 6
+        small = rng.integers(1, 9, n).tolist()
+        big = rng.integers(1, 300, n).tolist()
+        M, N = (small, big) if thin == "M" else (big, small)
+        K = rng.integers(0, 90, n).tolist()
+        c = Case(layout, ta, tb, M, N, K, seed=cfg)
+        pA, pB, pC = c.ptrs()
+        with bg.Plan(M, N, K, c.lda, c.ldb, c.ldc, mode="simt", layout=layout, trans_a=ta,
+                     trans_b=tb, force_tile_config=cfg) as p:
+            assert p.info()["tile_config_hist"][cfg] == n
+            p.execute(0.5, pA, pB, -1.5, pC)
+            torch.cuda.synchronize()
+        for i, (g, w) in enumerate(zip(c.result(), c.expected_f32(0.5, -1.5))):
+            np.testing.assert_array_equal(np.ascontiguousarray(g).view(np.uint32),
+                                          np.ascontiguousarray(w).view(np.uint32),
+                                          err_msg="cfg %d matrix %d %s" % (cfg, i, (layout, ta, tb)))
