@@ -415,7 +415,7 @@ extern "C" bgemm_status_t bgemm_framework_gemm_mode(const int* dM, const int* dN
   if (e != cudaSuccess) return cuda_error(e, "tensor-map build launch");
   TcPackParams pp{s.descs, s.pdescs, s.jobs, 0, s.counts + 1, kind, split, s.ws,
                   const_cast<const float* const*>(dA), const_cast<const float* const*>(dB)};
-  e = tc_pack_launch(pp, df.num_sms * 8, stream);
+  e = tc_pack_launch(pp, df.num_sms * kPackCtasPerSm, stream);
   if (e != cudaSuccess) return cuda_error(e, "split/pack launch");
   TcGemmParams gp{s.descs, s.items, 0, s.counts, s.counters, s.tmaps, 1.0f, 1.0f, dC,
                   s.gemm_err, 2000000000ull, nullptr, tc_schedule(mode)};

@@ -12,6 +12,8 @@ namespace bgemm {
 
 // Element kinds of the packed operands.
 enum TcKind : int { kKindTF32 = 0, kKindBF16 = 1 };
+// Split pre-pass grid: CTAs per SM (about five waves of the three resident).
+constexpr int kPackCtasPerSm = 16;
 
 // Tile configurations: UMMA M = 128 rows of the "A side" operand, UMMA N =
 // BN rows of the "B side".  Ids 0..3 keep A on the A side (BN 16/32/64/128);

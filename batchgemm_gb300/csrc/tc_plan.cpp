@@ -295,8 +295,10 @@ bgemm_status_t tc_alloc(bgemm_plan_s* p) {
   t->d_pdescs = reinterpret_cast<PackDesc*>(dm + t->off_pd);
   t->d_jobs = reinterpret_cast<PackJob*>(dm + t->off_jobs);
   t->d_err = reinterpret_cast<int*>(dm + t->off_err);
+  // 16 CTAs per SM, ~5 waves of the 3 that fit: a shorter last wave than 8 per
+  // SM (measured: the skewed pre-pass 3.03 -> 2.98 ms; 4 per SM, 1.3 waves, 3.63)
   t->pack_grid = (int)std::max<long long>(
-      1, std::min<long long>(t->cap_jobs, (long long)p->facts.num_sms * 8));
+      1, std::min<long long>(t->cap_jobs, (long long)p->facts.num_sms * kPackCtasPerSm));
   p->info.workspace_bytes = t->cap_ws;
   p->info.device_bytes += t->cap_ws + t->mem_bytes;
   p->info.kernels_per_execute = 2;
