@@ -8,7 +8,9 @@
 // launched for a tile outside its matrix.
 //
 // Each item is one BM x BN output tile of one matrix.  256 threads form a
-// 16 x 16 grid; each owns a TM x TN register tile.  Operands stream through a
+// 16 x 16 grid; each owns a TM x TN register tile (the thin 8 x 128 and
+// 128 x 8 tiles, simt_thin, give each thread four outputs along the thin
+// side instead).  Operands stream through a
 // cp.async ring of BK = 16 k-slices (4 stages for 128 x 128 tiles, up to the
 // autotuned kSimtRingCap for smaller ones):
 //   A slice: [k][BM]     (column of A, 16-byte cp.async when lda % 4 == 0 and
