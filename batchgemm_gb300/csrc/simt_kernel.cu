@@ -426,8 +426,14 @@ __device__ __forceinline__ void simt_thin(const MatDesc& d, int tm, int tn,
   constexpr int BN = THIN_M ? 128 : 8;
   constexpr int LDAS = BM + kPadB;  // rows of k padded like the transposed loads
   constexpr int LDBS = BN + kPadB;
+  // 8 x 128 tiles of the reference layout keep B's slice as [n][k]: each
+  // column's 16 k arrive as four 16-byte copies (B is k-contiguous), and each
+  // thread reads its own column four k at a time.  Rows of 20 floats keep
+  // those float4 reads of eight lanes on distinct banks.
+  constexpr bool KMAJ = THIN_M && !GEN;
+  constexpr int LDK = kBK + 4;
   constexpr int A_STAGE = kBK * LDAS;
-  constexpr int STAGE = A_STAGE + kBK * LDBS;
+  constexpr int STAGE = A_STAGE + (KMAJ ? BN * LDK : kBK * LDBS);
   constexpr int NS = ring_stages<GEN>(STAGE);
   static_assert(NS >= kStages, "ring of at least kStages stages");
   const int tid = threadIdx.x;
@@ -443,6 +449,7 @@ __device__ __forceinline__ void simt_thin(const MatDesc& d, int tm, int tn,
   const bool ta = GEN && (d.aux & kTransAFlag), tb = GEN && (d.aux & kTransBFlag);
   const bool a_vec = !ta && ((reinterpret_cast<uintptr_t>(A) & 15u) == 0) && ((d.lda & 3) == 0);
   const bool b_vec = tb && ((reinterpret_cast<uintptr_t>(B) & 15u) == 0) && ((d.ldb & 3) == 0);
+  const bool b_vec_k = KMAJ && ((reinterpret_cast<uintptr_t>(B) & 15u) == 0) && ((d.ldb & 3) == 0);
   auto load_stage = [&](int kb, int slot) {
     float* sA = smem + slot * STAGE;
     float* sB = sA + A_STAGE;
@@ -451,6 +458,29 @@ __device__ __forceinline__ void simt_thin(const MatDesc& d, int tm, int tn,
       load_rows_contig<BM, LDAS>(A, lda, M, m0, k0, K, sA, a_vec, tid);
     else
       load_k_contig<BM, LDAS>(A, lda, M, m0, k0, K, sA, tid);
+    if constexpr (KMAJ) {
+      if (b_vec_k) {
+#pragma unroll
+        for (int c0 = 0; c0 < BN * 4; c0 += kThreads) {
+          const int c = c0 + tid;
+          const int nn = c >> 2, kq = (c & 3) * 4;
+          const int gn = n0 + nn, gk = k0 + kq;
+          const int valid = (gn < N) ? min(max(K - gk, 0), 4) : 0;
+          const float* src = valid ? B + (long long)gn * ldb + gk : B;
+          cp_async16(smem_u32(sB + nn * LDK + kq), src, valid * 4);
+        }
+      } else {
+#pragma unroll
+        for (int e0 = 0; e0 < BN * kBK; e0 += kThreads) {
+          const int e = e0 + tid;
+          const int kk = e & (kBK - 1), nn = e / kBK;
+          const int gk = k0 + kk, gn = n0 + nn;
+          const bool v = (gk < K) && (gn < N);
+          cp_async4(smem_u32(sB + nn * LDK + kk), v ? B + (long long)gn * ldb + gk : B, v ? 4 : 0);
+        }
+      }
+      return;
+    }
     if (tb)
       load_rows_contig<BN, LDBS>(B, ldb, N, n0, k0, K, sB, b_vec, tid);
     else
@@ -479,6 +509,22 @@ __device__ __forceinline__ void simt_thin(const MatDesc& d, int tm, int tn,
     }
     const float* sA = smem + (kb % NS) * STAGE;
     const float* sB = sA + A_STAGE;
+    if constexpr (KMAJ) {
+#pragma unroll
+      for (int k = 0; k < kBK; k += 4) {
+        const float4 b4 = *reinterpret_cast<const float4*>(sB + own * LDK + k);
+        const float bk[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          const float4 a = *reinterpret_cast<const float4*>(sA + (k + kk) * LDAS + 4 * quad);
+          acc[0] = fmaf(a.x, bk[kk], acc[0]);
+          acc[1] = fmaf(a.y, bk[kk], acc[1]);
+          acc[2] = fmaf(a.z, bk[kk], acc[2]);
+          acc[3] = fmaf(a.w, bk[kk], acc[3]);
+        }
+      }
+      continue;
+    }
 #pragma unroll
     for (int k = 0; k < kBK; ++k) {
       if constexpr (THIN_M) {
