@@ -501,7 +501,7 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       if (!ok) break;
       it = fetch();
       if constexpr (BETA)
-        c_store<kCols, 16>(r, C, ldc, d.M, d.N, swap, row0, col_base, ncols, alpha, beta, lane);
+        c_store_pipe<kCols, 8>(r, C, ldc, d.M, d.N, swap, row0, col_base, ncols, alpha, beta, lane);
       else
         c_store<kCols>(r, C, ldc, d.M, d.N, swap, row0, col_base, ncols, alpha, beta, lane);
     }
