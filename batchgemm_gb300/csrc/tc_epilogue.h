@@ -137,10 +137,16 @@ __device__ __forceinline__ void c_store_pipe(float (&r)[COLS], float* C, long lo
     int m, n0, nlim;
     bool ok;
     if (!swap) {
-      m = row0 + lane; n0 = col_base + c0; nlim = min(N - n0, ncols - c0); ok = m < M;
+      m = row0 + lane;
+      n0 = col_base + c0;
+      nlim = min(N - n0, ncols - c0);
+      ok = m < M;
     } else {
       warp_transpose32(r, c0, lane);
-      m = col_base + c0 + lane; n0 = row0; nlim = N - n0; ok = (c0 + lane < ncols) && m < M;
+      m = col_base + c0 + lane;
+      n0 = row0;
+      nlim = N - n0;
+      ok = (c0 + lane < ncols) && m < M;
     }
     float* base = C + m + (long long)n0 * ldc;
     float cv[2][NRD];
