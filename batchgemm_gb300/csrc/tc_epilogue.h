@@ -12,8 +12,9 @@
 // With beta != 0 the old C is read.  c_prefetch pulls those lines into L2
 // ahead of c_store (the one-SM kernel when a tile starts, the CTA-pair kernel
 // two promotion groups before a tile ends: earlier, the operand stream evicts
-// them again), so the final reads (issued in groups, all before the stores
-// of their group) hit L2 instead of waiting on HBM per element.
+// them again), so the final reads (issued in groups before the stores of
+// their group; pipelined one group ahead in the CTA-pair kernel) hit L2
+// instead of waiting on HBM per element.
 #pragma once
 #include <stdint.h>
 
@@ -167,4 +168,5 @@ __device__ __forceinline__ void c_store_pipe(float (&r)[COLS], float* C, long lo
     }
   }
 }
+
 }  // namespace bgemm
