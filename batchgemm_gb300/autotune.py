@@ -246,7 +246,7 @@ def current_tables():
     return simt, tc, sched, params
 
 
-BUILD_CANDIDATES = {"simt_ring_cap": [4, 6, 8], "c_prefetch_lead": [1, 2, 3, 4]}
+BUILD_CANDIDATES = {"simt_ring_cap": [4, 6, 8], "c_prefetch_lead": [0, 1, 2, 3, 4]}
 
 
 def measure_build_params(which, reps=5):

@@ -83,7 +83,7 @@ __device__ __forceinline__ int group_slices(const TcGemmParams& p, int K) {
   return p.sched.group(tc_sched_bucket(K));
 }
 // beta != 0: promotion groups before the tile's end at which C is prefetched
-// (autotuned, tile_table.h)
+// into L2 (autotuned, tile_table.h; 0 = no prefetch)
 constexpr int kCPrefetchLead = kTcCPrefetchLead;
 static_assert(kCPrefetchLead >= 0 && kCPrefetchLead <= 16, "C prefetch lead out of range");
 
@@ -461,8 +461,8 @@ __global__ void __launch_bounds__(kThreads2, 1) tc2_gemm_kernel(const TcGemmPara
       int ok = 1;
       // beta != 0: C is pulled into L2 kCPrefetchLead groups before the tile
       // ends (earlier, the operand stream evicts it again before c_store)
-      const int g_pf = BETA ? max(0, ngroups - kCPrefetchLead) : -1;
-      if (BETA && ngroups == 0)
+      const int g_pf = (BETA && kCPrefetchLead > 0) ? max(0, ngroups - kCPrefetchLead) : -1;
+      if (BETA && kCPrefetchLead > 0 && ngroups == 0)
         c_prefetch<kCols>(C, ldc, d.M, d.N, swap, row0, col_base, ncols, lane);
       // buffers of up to P = 256 / bn promotion groups each (see the MMA lane);
       // the groups are added in K order, as if each had a buffer of its own

@@ -76,10 +76,11 @@ constexpr unsigned char kTcGroupTable[3][8] = {
 //                     many 16-k stages as the CTA's shared memory holds, up
 //                     to this cap (the 128 x 128 tile always has 4);
 //   kTcCPrefetchLead  beta != 0: promotion groups before the end of a pair
-//                     tile at which its C lines are prefetched into L2.
+//                     tile at which its C lines are prefetched into L2 (0:
+//                     none; the epilogue's pipelined reads then go to HBM).
 #if !defined(BGEMM_TUNED_HAS_BUILD_PARAMS)
 constexpr int kSimtRingCap = 4;
-constexpr int kTcCPrefetchLead = 2;
+constexpr int kTcCPrefetchLead = 0;
 #endif
 
 }  // namespace bgemm
