@@ -9,12 +9,13 @@
 // transposed across the warp with shuffles, after which lanes again walk
 // consecutive m.
 //
-// With beta != 0 the old C is read.  c_prefetch pulls those lines into L2
-// ahead of c_store (the one-SM kernel when a tile starts, the CTA-pair kernel
-// two promotion groups before a tile ends: earlier, the operand stream evicts
-// them again), so the final reads (issued in groups before the stores of
-// their group; pipelined one group ahead in the CTA-pair kernel) hit L2
-// instead of waiting on HBM per element.
+// With beta != 0 the old C is read.  In the one-SM kernel c_prefetch pulls
+// those lines into L2 when a tile starts, so the final reads (issued in
+// groups before the stores of their group) hit L2 instead of waiting on HBM
+// per element.  The CTA-pair kernel prefetches only if its autotuned lead is
+// nonzero (measured: none is fastest -- the prefetched lines displace operand
+// lines the MMA still needs) and pipelines its reads one group ahead of the
+// stores (c_store_pipe).
 #pragma once
 #include <stdint.h>
 
