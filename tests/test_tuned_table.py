@@ -85,3 +85,30 @@ def test_build_params_in_table_and_library(built_lib):
     assert ring in autotune.BUILD_CANDIDATES["simt_ring_cap"]
     assert lead in autotune.BUILD_CANDIDATES["c_prefetch_lead"]
     assert L.bgemm_debug_build_params(None, ctypes.byref(c)) == -1
+
+
+def test_write_table_round_trip(tmp_path):
+    """autotune.write_table emits every table the library compiles in; the
+    values read back from the text are the ones written."""
+    simt = [(1000.0 + c, 10.0 + c) for c in range(len(autotune.SIMT_CFGS))]
+    tc = {m: [((2000.0 + c, 5.0 + c) if c != 11 else None) for c in range(16)]
+          for m in ("tf32", "tf32x3", "bf16x3")}
+    sched = {"tf32": [0, 2, 2, 2, 2, 2, 2, 2], "tf32x3": [0, 1, 1, 1, 2, 3, 4, 4],
+             "bf16x3": [0, 0, 3, 3, 4, 4, 4, 4]}
+    params = {"simt_ring_cap": 6, "c_prefetch_lead": 0}
+    out = tmp_path / "t.inc"
+    autotune.write_table(str(out), simt, tc, sched, "test device", 152, params)
+    text = out.read_text()
+    rows = re.findall(r"\{([\d.]+)f, ([\d.]+)f\}", text.split("kSimtCost")[1].split(";")[0])
+    assert [(float(a), float(b)) for a, b in rows] == simt
+    tc_text = text.split("kTcCost")[1].split(";")[0]
+    vals = re.findall(r"\{([\d.]+)f, ([\d.]+)f\}", tc_text)
+    assert len(vals) == 48
+    assert (float(vals[16 + 11][0]), float(vals[16 + 11][1])) == (0.0, 0.0)  # no such tile
+    assert (float(vals[16 + 3][0]), float(vals[16 + 3][1])) == (2003.0, 8.0)
+    g = re.search(r"kTcGroupTable\[3\]\[8\] = \{(.*)\};", text).group(1)
+    assert [[int(x) for x in r.split(",")] for r in re.findall(r"\{([^{}]*)\}", g)] == [
+        sched["tf32"], sched["tf32x3"], sched["bf16x3"]]
+    assert "kSimtRingCap = 6;" in text and "kTcCPrefetchLead = 0;" in text
+    assert "#define BGEMM_TUNED_HAS_SCHEDULE 1" in text
+    assert "#define BGEMM_TUNED_HAS_BUILD_PARAMS 1" in text
